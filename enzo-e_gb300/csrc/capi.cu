@@ -1,0 +1,638 @@
+// capi.cu -- C ABI: parameters, handle and the per-block Method operations
+// (EnzoMethodMHDVlct::compute / ::timestep and the ghost refresh).
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "capi_internal.h"
+#include "vlct_aux.cuh"
+
+using namespace vlct;
+
+namespace mhdint {
+
+int fail(mhdvlct_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+static std::string lower(const char* s) {
+  std::string o(s ? s : "");
+  for (auto& c : o) c = (char)std::tolower((unsigned char)c);
+  return o;
+}
+
+StagePlan stage_plan(const mhdvlct_handle* h) {
+  StagePlan p;
+  auto imm = [](int r) { return r == RECON_NN ? 0 : 1; };
+  auto tot = [](int r) { return r == RECON_NN ? 1 : 2; };
+  if (h->euler) {
+    p.nstages = 1;
+    p.recon[0] = h->recon;
+    p.s[0] = 0;
+    p.S[0] = imm(h->recon);
+    p.dt_factor[0] = 1.0;
+  } else {
+    p.nstages = 2;
+    p.recon[0] = RECON_NN;
+    p.recon[1] = h->recon;
+    p.s[0] = 0;
+    p.S[0] = 0;
+    p.dt_factor[0] = 0.5;
+    p.s[1] = tot(RECON_NN);
+    p.S[1] = p.s[1] + imm(h->recon);
+    p.dt_factor[1] = 1.0;
+  }
+  return p;
+}
+
+// near-equal split of [lo, hi) into parts of at most t
+static void split(int lo, int hi, int t, std::vector<std::pair<int, int>>& out) {
+  out.clear();
+  const int len = hi - lo;
+  if (len <= 0) return;
+  if (t <= 0 || t > len) t = len;
+  const int n = (len + t - 1) / t;
+  int a = lo;
+  for (int i = 0; i < n; i++) {
+    const int w = len / n + (i < len % n ? 1 : 0);
+    out.push_back({a, a + w});
+    a += w;
+  }
+}
+
+void make_tiles(int block, const int m[3], int S, bool final, int tile_x,
+                int tile_y, int zchunk, std::vector<StageTile>& out) {
+  const int lo = final ? S : S + 1;
+  const int hi_x = final ? m[0] - S : m[0] - S - 1;
+  const int hi_y = final ? m[1] - S : m[1] - S - 1;
+  const int hi_z = final ? m[2] - S : m[2] - S - 1;
+  std::vector<std::pair<int, int>> xs, ys, zs;
+  split(lo, hi_x, tile_x, xs);
+  split(lo, hi_y, tile_y, ys);
+  split(lo, hi_z, zchunk > 0 ? zchunk : (hi_z - lo), zs);
+  for (auto& z : zs)
+    for (auto& y : ys)
+      for (auto& x : xs)
+        out.push_back({block, x.first, x.second, y.first, y.second, z.first, z.second});
+}
+
+template <class R>
+FieldSet<R> fieldset_of(const MhdBlockView* b) {
+  FieldSet<R> f;
+  f.c[F_RHO] = (R*)b->density;
+  f.c[F_VX] = (R*)b->velocity[0];
+  f.c[F_VY] = (R*)b->velocity[1];
+  f.c[F_VZ] = (R*)b->velocity[2];
+  f.c[F_ETOT] = (R*)b->total_energy;
+  f.c[F_EINT] = (R*)b->internal_energy;
+  f.c[F_BX] = (R*)b->bfield[0];
+  f.c[F_BY] = (R*)b->bfield[1];
+  f.c[F_BZ] = (R*)b->bfield[2];
+  for (int d = 0; d < 3; d++) f.f[d] = (R*)b->bfieldi[d];
+  return f;
+}
+template FieldSet<double> fieldset_of<double>(const MhdBlockView*);
+template FieldSet<float> fieldset_of<float>(const MhdBlockView*);
+
+int default_tile(int dtype, int solver, int recon, int de) {
+  // largest tile whose shared memory fits two CTAs' worth under 227 KB for
+  // FP32 and one CTA for FP64
+  const int cap = (dtype == MHD_DTYPE_F64) ? 200 * 1024 : 110 * 1024;
+  int best = 4;
+  for (int t = 4; t <= (dtype == MHD_DTYPE_F64 ? TileLimits<double>::TMAX
+                                                 : TileLimits<float>::TMAX);
+       t++) {
+    const size_t b = (dtype == MHD_DTYPE_F64)
+                         ? stage_smem<double>(solver, recon, de != 0, t, t)
+                         : stage_smem<float>(solver, recon, de != 0, t, t);
+    if (b <= (size_t)cap) best = t;
+  }
+  return best;
+}
+
+}  // namespace mhdint
+
+using namespace mhdint;
+
+// ------------------------------------------------------------------ params
+extern "C" void mhdvlct_params_default(MhdVlctParams* p) {
+  std::memset(p, 0, sizeof(*p));
+  std::snprintf(p->riemann_solver, sizeof(p->riemann_solver), "hlld");
+  std::snprintf(p->time_scheme, sizeof(p->time_scheme), "vl");
+  std::snprintf(p->reconstruct_method, sizeof(p->reconstruct_method), "plm");
+  p->theta_limiter = 1.5;
+  p->courant = -1.0;  // resolved from time_scheme at create (vl: 0.3, euler: 1)
+  p->gamma = 5.0 / 3.0;
+  p->density_floor = 0.0;
+  p->pressure_floor = 0.0;
+  p->dual_energy = 0;
+  p->dual_energy_eta = 0.001;
+}
+
+namespace {
+// Minimal reader of the Cello parameter language subset used by this
+// method: nested groups `Name { ... }`, assignments `key = value;` with
+// string, number or logical values.  Produces dotted paths such as
+// "Method:mhd_vlct:riemann_solver".
+struct PTok {
+  std::string path, value;
+  bool is_string;
+};
+static bool parse_params(const char* text, std::vector<PTok>& out,
+                         std::string& err) {
+  std::vector<std::string> stack;
+  const char* c = text;
+  auto skip = [&]() {
+    for (;;) {
+      while (*c && std::isspace((unsigned char)*c)) c++;
+      if (*c == '#') {
+        while (*c && *c != '\n') c++;
+        continue;
+      }
+      break;
+    }
+  };
+  std::string pending;
+  for (;;) {
+    skip();
+    if (!*c) break;
+    if (*c == '}') {
+      if (stack.empty()) { err = "unbalanced '}'"; return false; }
+      stack.pop_back();
+      c++;
+      skip();
+      if (*c == ';') c++;
+      continue;
+    }
+    if (*c == ';') { c++; continue; }
+    const char* s0 = c;
+    while (*c && (std::isalnum((unsigned char)*c) || *c == '_' || *c == ':')) c++;
+    std::string ident(s0, c);
+    if (ident.empty()) { err = std::string("unexpected character '") + *c + "'"; return false; }
+    skip();
+    if (*c == '{') {
+      stack.push_back(ident);
+      c++;
+      continue;
+    }
+    if (*c != '=') { err = "expected '=' after " + ident; return false; }
+    c++;
+    skip();
+    PTok t;
+    std::string path;
+    for (auto& s : stack) path += s + ":";
+    t.path = path + ident;
+    t.is_string = false;
+    if (*c == '"') {
+      c++;
+      const char* v0 = c;
+      while (*c && *c != '"') c++;
+      if (*c != '"') { err = "unterminated string"; return false; }
+      t.value.assign(v0, c);
+      t.is_string = true;
+      c++;
+    } else if (*c == '[') {  // lists are skipped
+      int depth = 0;
+      do {
+        if (*c == '[') depth++;
+        if (*c == ']') depth--;
+        c++;
+      } while (*c && depth > 0);
+    } else {
+      const char* v0 = c;
+      while (*c && *c != ';' && *c != '}' && !std::isspace((unsigned char)*c)) c++;
+      t.value.assign(v0, c);
+    }
+    skip();
+    if (*c == ';') c++;
+    out.push_back(t);
+  }
+  if (!stack.empty()) { err = "unbalanced '{'"; return false; }
+  return true;
+}
+}  // namespace
+
+extern "C" int mhdvlct_params_parse(const char* text, MhdVlctParams* out,
+                                    char* errbuf, size_t errbuf_len) {
+  auto report = [&](const std::string& m) {
+    if (errbuf && errbuf_len) std::snprintf(errbuf, errbuf_len, "%s", m.c_str());
+    return MHD_ERR_INVALID;
+  };
+  if (!text || !out) return report("null argument");
+  mhdvlct_params_default(out);
+  std::vector<PTok> toks;
+  std::string err;
+  if (!parse_params(text, toks, err)) return report(err);
+  for (const auto& t : toks) {
+    const std::string& k = t.path;
+    auto num = [&](double* dst) -> bool {
+      char* end = nullptr;
+      const double v = std::strtod(t.value.c_str(), &end);
+      if (!end || *end) return false;
+      *dst = v;
+      return true;
+    };
+    auto str = [&](char* dst, size_t n) -> bool {
+      if (!t.is_string || t.value.size() + 1 > n) return false;
+      std::snprintf(dst, n, "%s", t.value.c_str());
+      return true;
+    };
+    bool ok = true;
+    if (k == "Method:mhd_vlct:mhd_choice") ok = str(out->mhd_choice, sizeof(out->mhd_choice));
+    else if (k == "Method:mhd_vlct:riemann_solver") ok = str(out->riemann_solver, sizeof(out->riemann_solver));
+    else if (k == "Method:mhd_vlct:time_scheme") ok = str(out->time_scheme, sizeof(out->time_scheme));
+    else if (k == "Method:mhd_vlct:reconstruct_method") ok = str(out->reconstruct_method, sizeof(out->reconstruct_method));
+    else if (k == "Method:mhd_vlct:theta_limiter") ok = num(&out->theta_limiter);
+    else if (k == "Method:mhd_vlct:courant") ok = num(&out->courant);
+    else if (k == "Physics:fluid_props:eos:gamma") ok = num(&out->gamma);
+    else if (k == "Physics:fluid_props:floors:density") ok = num(&out->density_floor);
+    else if (k == "Physics:fluid_props:floors:pressure") ok = num(&out->pressure_floor);
+    else if (k == "Physics:fluid_props:dual_energy:eta") ok = num(&out->dual_energy_eta);
+    else if (k == "Physics:fluid_props:dual_energy:type") {
+      const std::string v = lower(t.value.c_str());
+      if (v == "modern") out->dual_energy = 1;
+      else if (v == "disabled" || v == "none") out->dual_energy = 0;
+      else return report("dual_energy:type \"" + t.value + "\" is not supported");
+    } else if (k == "Method:mhd_vlct:half_dt_reconstruct_method" ||
+               k == "Method:mhd_vlct:full_dt_reconstruct_method") {
+      // removed parameters (EnzoMethodMHDVlct.cpp:62-70)
+      return report(k + " has been removed; use reconstruct_method");
+    }
+    if (!ok) return report("bad value for " + k + ": " + t.value);
+  }
+  return MHD_OK;
+}
+
+// ------------------------------------------------------------------ handle
+extern "C" int mhdvlct_create(const MhdVlctParams* p, mhdvlct_handle** out) {
+  if (!p || !out) return MHD_ERR_INVALID;
+  *out = nullptr;
+  mhdvlct_handle* h = new mhdvlct_handle();
+  h->params = *p;
+  auto bad = [&](const std::string& m) {
+    // keep the handle so the caller can read the message, but signal failure
+    h->err = m;
+    *out = h;
+    return MHD_ERR_INVALID;
+  };
+  const std::string choice = lower(p->mhd_choice);
+  if (choice.empty()) return bad("Method:mhd_vlct:mhd_choice wasn't specified");
+  if (choice == "no_bfield") h->mhd = 0;
+  else if (choice == "constrained_transport") h->mhd = 1;
+  else if (choice == "unsafe_constant_uniform")
+    return bad("unsafe_constant_uniform is for debugging only and is not supported");
+  else return bad("Unrecognized mhd_choice \"" + std::string(p->mhd_choice) + "\"");
+  // EnzoRiemann::construct_riemann (riemann/EnzoRiemann.cpp:26-68)
+  const std::string rs = lower(p->riemann_solver);
+  if (rs == "hlld") {
+    if (!h->mhd) return bad("The \"HLLD\" Riemann Solver requires magnetic fields");
+    h->solver = SOLVER_HLLD;
+  } else if (rs == "hlle") {
+    if (!h->mhd) return bad("The \"HLLE\" Riemann solver without magnetic fields is untested");
+    h->solver = SOLVER_HLLE;
+  } else if (rs == "hllc") {
+    if (h->mhd) return bad("The \"HLLC\" Riemann Solver can't support mhd");
+    h->solver = SOLVER_HLLC;
+  } else if (rs == "hll") {
+    return bad("The \"HLL\" (Davis wave speed) solver is untested in the reference");
+  } else {
+    return bad("The only known solvers are HLL, HLLE, HLLC, & HLLD");
+  }
+  // EnzoReconstructor::construct_reconstructor (toolkit/EnzoReconstructor.cpp:14-44)
+  if (!(1. <= p->theta_limiter && p->theta_limiter <= 2.))
+    return bad("theta_limiter must satisfy 1<=theta_limiter<=2");
+  const std::string rc = lower(p->reconstruct_method);
+  if (rc == "nn") h->recon = RECON_NN;
+  else if (rc == "plm" || rc == "plm_enzo") h->recon = RECON_PLM;
+  else if (rc == "plm_athena") h->recon = RECON_PLM_ATHENA;
+  else return bad("The only allowed reconstructors are NN, PLM, PLM_ENZO, & PLM_ATHENA");
+  const std::string ts = lower(p->time_scheme);
+  if (ts == "vl") h->euler = 0;
+  else if (ts == "euler") h->euler = 1;
+  else return bad("time_scheme must be \"vl\" or \"euler\"");
+  if (h->params.courant < 0) h->params.courant = h->euler ? 1.0 : 0.3;
+  if (!(p->gamma > 1.0)) return bad("gamma should exceed 1.0");
+  // EnzoMHDIntegratorStageCommands ctor (EnzoMHDIntegratorStageCommands.cpp:35-40)
+  if (!(p->density_floor > 0) || !(p->pressure_floor > 0))
+    return bad("density and pressure floors must be defined");
+  h->de = p->dual_energy ? 1 : 0;
+  if (h->de && !(p->dual_energy_eta >= 0)) return bad("eta must be non-negative");
+  h->phys.gamma = p->gamma;
+  h->phys.density_floor = p->density_floor;
+  h->phys.pressure_floor = p->pressure_floor;
+  h->phys.theta_limiter = p->theta_limiter;
+  h->phys.eta = h->de ? p->dual_energy_eta : 0.0;
+  *out = h;
+  return MHD_OK;
+}
+
+extern "C" int mhdvlct_destroy(mhdvlct_handle* h) {
+  if (!h) return MHD_ERR_INVALID;
+  if (h->scratch) cudaFree(h->scratch);
+  delete h;
+  return MHD_OK;
+}
+
+extern "C" const char* mhdvlct_last_error_string(const mhdvlct_handle* h) {
+  return h ? h->err.c_str() : "null handle";
+}
+
+extern "C" double mhdvlct_courant(const mhdvlct_handle* h) {
+  return h ? h->params.courant : -1.0;
+}
+
+extern "C" int mhdvlct_required_ghost_depth(const mhdvlct_handle* h) {
+  if (!h) return -1;
+  const StagePlan sp = stage_plan(h);
+  int g = 0;
+  for (int i = 0; i < sp.nstages; i++) g += (sp.recon[i] == RECON_NN) ? 1 : 2;
+  return g;
+}
+
+// -------------------------------------------------------------- one block
+namespace {
+
+int check_view(mhdvlct_handle* h, const MhdBlockView* b) {
+  if (!b) return fail(h, MHD_ERR_INVALID, "null block view");
+  if (b->dtype != MHD_DTYPE_F64 && b->dtype != MHD_DTYPE_F32)
+    return fail(h, MHD_ERR_INVALID, "unknown dtype");
+  if (b->ghost[0] != b->ghost[1] || b->ghost[0] != b->ghost[2])
+    return fail(h, MHD_ERR_INVALID, "ghost depth must be equal on all axes");
+  if (b->ghost[0] < mhdvlct_required_ghost_depth(h))
+    return fail(h, MHD_ERR_GHOST,
+                "ghost depth must be at least " +
+                    std::to_string(mhdvlct_required_ghost_depth(h)));
+  for (int a = 0; a < 3; a++) {
+    if (b->n[a] < 1) return fail(h, MHD_ERR_INVALID, "block extents must be positive");
+    if (!(b->cell_width[a] > 0)) return fail(h, MHD_ERR_INVALID, "cell widths must be positive");
+    if (b->n[a] + 2 * b->ghost[a] > 4096) return fail(h, MHD_ERR_INVALID, "block too large");
+  }
+  if (!b->density || !b->velocity[0] || !b->velocity[1] || !b->velocity[2] ||
+      !b->total_energy)
+    return fail(h, MHD_ERR_INVALID, "missing hydro field pointer");
+  if (h->de && !b->internal_energy)
+    return fail(h, MHD_ERR_INVALID, "internal_energy is required with dual energy");
+  if (h->mhd) {
+    for (int d = 0; d < 3; d++)
+      if (!b->bfield[d] || !b->bfieldi[d])
+        return fail(h, MHD_ERR_INVALID, "missing bfield / bfieldi pointer");
+  }
+  return MHD_OK;
+}
+
+int cuda_fail(mhdvlct_handle* h, cudaError_t e, const char* where) {
+  return fail(h, MHD_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Scratch of the plain path, carved from one allocation.
+template <class R> struct PlainScratch {
+  R* tmp[NCELL];
+  R* tface[3];
+  R* fface[3];
+  double* d_dt;
+  double* d_dtout;
+  void* d_smax;
+  StageBlock<R>* d_sblocks;  // [2]
+  AuxBlock<R>* d_aux;        // [1]
+  int* d_nbr;                // [27]
+  StageTile* d_tiles;        // stage 0 tiles then stage 1 tiles
+  int ntiles[2];
+};
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+template <class R>
+int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
+                   PlainScratch<R>& S, cudaStream_t st) {
+  const StagePlan sp = stage_plan(h);
+  if (h->tile <= 0) h->tile = 8;
+  std::vector<StageTile> tiles[2];
+  for (int i = 0; i < sp.nstages; i++)
+    make_tiles(0, m, sp.S[i], i + 1 == sp.nstages, h->tile, h->tile, h->zchunk,
+               tiles[i]);
+  const size_t M = (size_t)m[0] * m[1] * m[2];
+  const size_t F[3] = {(size_t)(m[0] + 1) * m[1] * m[2],
+                       (size_t)m[0] * (m[1] + 1) * m[2],
+                       (size_t)m[0] * m[1] * (m[2] + 1)};
+  size_t off = 0;
+  std::vector<size_t> offs;
+  auto take = [&](size_t bytes) { offs.push_back(off); off += align_up(bytes); };
+  for (int k = 0; k < NCELL; k++) take(M * sizeof(R));
+  for (int d = 0; d < 3; d++) take(F[d] * sizeof(R));
+  for (int d = 0; d < 3; d++) take(F[d] * sizeof(R));
+  take(sizeof(double));
+  take(sizeof(double));
+  take(3 * sizeof(unsigned long long));
+  take(2 * sizeof(StageBlock<R>));
+  take(sizeof(AuxBlock<R>));
+  take(27 * sizeof(int));
+  take((tiles[0].size() + tiles[1].size()) * sizeof(StageTile));
+  const bool same = h->scratch && h->cache_dtype == dtype && h->cache_m[0] == m[0] &&
+                    h->cache_m[1] == m[1] && h->cache_m[2] == m[2] &&
+                    h->scratch_bytes >= off;
+  if (!same) {
+    if (h->scratch) {
+      cudaStreamSynchronize(st);
+      cudaFree(h->scratch);
+      h->scratch = nullptr;
+    }
+    cudaError_t e = cudaMalloc(&h->scratch, off);
+    if (e != cudaSuccess) {
+      h->scratch = nullptr;
+      return fail(h, MHD_ERR_NOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
+    }
+    h->scratch_bytes = off;
+    h->cache_dtype = dtype;
+    for (int a = 0; a < 3; a++) h->cache_m[a] = m[a];
+  }
+  char* base = (char*)h->scratch;
+  int i = 0;
+  for (int k = 0; k < NCELL; k++) S.tmp[k] = (R*)(base + offs[i++]);
+  for (int d = 0; d < 3; d++) S.tface[d] = (R*)(base + offs[i++]);
+  for (int d = 0; d < 3; d++) S.fface[d] = (R*)(base + offs[i++]);
+  S.d_dt = (double*)(base + offs[i++]);
+  S.d_dtout = (double*)(base + offs[i++]);
+  S.d_smax = (void*)(base + offs[i++]);
+  S.d_sblocks = (StageBlock<R>*)(base + offs[i++]);
+  S.d_aux = (AuxBlock<R>*)(base + offs[i++]);
+  S.d_nbr = (int*)(base + offs[i++]);
+  S.d_tiles = (StageTile*)(base + offs[i++]);
+  S.ntiles[0] = (int)tiles[0].size();
+  S.ntiles[1] = (int)tiles[1].size();
+  if (!same) {
+    std::vector<StageTile> all(tiles[0]);
+    all.insert(all.end(), tiles[1].begin(), tiles[1].end());
+    cudaError_t e = cudaMemcpyAsync(S.d_tiles, all.data(), all.size() * sizeof(StageTile),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "tile upload");
+    std::vector<int> nbr(27, 0);
+    e = cudaMemcpyAsync(S.d_nbr, nbr.data(), 27 * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "neighbour upload");
+    // scratch cell fields that a block never writes must still be defined
+    e = cudaMemsetAsync(h->scratch, 0, offs[NCELL + 6], st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "scratch clear");
+  }
+  return MHD_OK;
+}
+
+template <class R>
+int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
+                 cudaStream_t st) {
+  const int g = b->ghost[0];
+  const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
+  PlainScratch<R> S;
+  int rc = ensure_scratch<R>(h, m, b->dtype, S, st);
+  if (rc) return rc;
+  const StagePlan sp = stage_plan(h);
+  FieldSet<R> ext = fieldset_of<R>(b);
+  FieldSet<R> tmp;
+  for (int k = 0; k < NCELL; k++) tmp.c[k] = S.tmp[k];
+  for (int d = 0; d < 3; d++) tmp.f[d] = S.tface[d];
+  const size_t M = (size_t)m[0] * m[1] * m[2];
+  cudaError_t e = launch_set_scalar(S.d_dt, dt, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "dt upload");
+
+  StageBlock<R> sb[2];
+  for (int i = 0; i < sp.nstages; i++) {
+    StageBlock<R>& B = sb[i];
+    for (int a = 0; a < 3; a++) {
+      B.m[a] = m[a];
+      B.cw[a] = b->cell_width[a];
+    }
+    B.dt = S.d_dt;
+    const bool final = (i + 1) == sp.nstages;
+    B.base = ext;
+    if (sp.nstages == 1) {
+      // euler: a single stage cannot update its own input in place, so it
+      // reads a copy of the block and writes into the caller's fields
+      B.cur = tmp;
+      for (int d = 0; d < 3; d++) B.cur.f[d] = ext.f[d];
+      B.out = ext;
+    } else if (i == 0) {
+      B.cur = ext;
+      B.out = tmp;
+    } else {
+      B.cur = tmp;
+      B.out = ext;
+    }
+    if (final) {
+      for (int d = 0; d < 3; d++) B.out.f[d] = S.fface[d];
+    }
+  }
+  e = cudaMemcpyAsync(S.d_sblocks, sb, sizeof(sb), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "block upload");
+  if (sp.nstages == 1) {
+    for (int k = 0; k < NCELL; k++) {
+      if (!ext.c[k]) continue;
+      e = cudaMemcpyAsync(S.tmp[k], ext.c[k], M * sizeof(R), cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
+    }
+  }
+  const StageTile* tiles[2] = {S.d_tiles, S.d_tiles + S.ntiles[0]};
+  for (int i = 0; i < sp.nstages; i++) {
+    StageInfo info;
+    info.s = sp.s[i];
+    info.S = sp.S[i];
+    info.final_stage = (i + 1) == sp.nstages;
+    info.dt_factor = sp.dt_factor[i];
+    info.tx = h->tile;
+    info.ty = h->tile;
+    e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, tiles[i],
+                        S.ntiles[i], info, h->phys, 0, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");
+  }
+  if (h->mhd) {
+    const int S1 = sp.S[sp.nstages - 1] + 1;
+    e = launch_copy_faces<R>(m[0], m[1], m[2], S1, S.fface[0], S.fface[1], S.fface[2],
+                             ext.f[0], ext.f[1], ext.f[2], st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "face copy");
+  }
+  return MHD_OK;
+}
+
+template <class R>
+int aux_setup(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
+              cudaStream_t st) {
+  const int g = b->ghost[0];
+  const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
+  int rc = ensure_scratch<R>(h, m, b->dtype, S, st);
+  if (rc) return rc;
+  AuxBlock<R> a;
+  for (int k = 0; k < 3; k++) {
+    a.m[k] = m[k];
+    a.cw[k] = b->cell_width[k];
+  }
+  a.f = fieldset_of<R>(b);
+  a.pressure = (R*)b->pressure;
+  cudaError_t e = cudaMemcpyAsync(S.d_aux, &a, sizeof(a), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "aux upload");
+  return MHD_OK;
+}
+
+template <class R>
+int block_timestep_t(mhdvlct_handle* h, const MhdBlockView* b, double* dt_out,
+                     cudaStream_t st) {
+  PlainScratch<R> S;
+  int rc = aux_setup<R>(h, b, S, st);
+  if (rc) return rc;
+  const int g = b->ghost[0];
+  const size_t M = (size_t)(b->n[0] + 2 * g) * (b->n[1] + 2 * g) * (b->n[2] + 2 * g);
+  const int chunks = (int)std::min<size_t>(std::max<size_t>(1, M / 1024), 1024);
+  cudaError_t e = launch_timestep<R>(h->mhd != 0, h->de != 0, S.d_aux, 1, chunks, h->phys,
+                                     S.d_smax, h->params.courant, 0, S.d_dtout, nullptr, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "timestep launch");
+  e = cudaMemcpyAsync(dt_out, S.d_dtout, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "dt download");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "timestep");
+  return MHD_OK;
+}
+
+template <class R>
+int fill_ghosts_t(mhdvlct_handle* h, const MhdBlockView* b, cudaStream_t st) {
+  PlainScratch<R> S;
+  int rc = aux_setup<R>(h, b, S, st);
+  if (rc) return rc;
+  cudaError_t e = launch_refresh<R>(S.d_aux, S.d_nbr, 1, b->ghost[0], 64, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "refresh launch");
+  return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b,
+                                  double dt, void* stream) {
+  if (!h) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, st)
+                                   : block_step_t<float>(h, b, dt, st);
+}
+
+extern "C" int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
+                                      double* dt_out, void* stream) {
+  if (!h || !dt_out) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? block_timestep_t<double>(h, b, dt_out, st)
+                                   : block_timestep_t<float>(h, b, dt_out, st);
+}
+
+extern "C" int mhdvlct_fill_ghosts_periodic(mhdvlct_handle* h, const MhdBlockView* b,
+                                            void* stream) {
+  if (!h) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? fill_ghosts_t<double>(h, b, st)
+                                   : fill_ghosts_t<float>(h, b, st);
+}

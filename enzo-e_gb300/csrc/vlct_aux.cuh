@@ -1,0 +1,287 @@
+// vlct_aux.cuh -- the kernels around the fused stages: the CFL timestep
+// reduction, the same-level ghost refresh gather and small copy helpers.
+#pragma once
+#include "vlct_physics.cuh"
+#include "vlct_types.h"
+
+namespace vlct {
+
+// A block as seen by the timestep and refresh kernels.
+template <class R> struct AuxBlock {
+  int m[3];
+  double cw[3];
+  FieldSet<R> f;     // fields (cell + face)
+  R* pressure;       // optional [w] pressure field
+};
+
+// ---------------------------------------------------------------------------
+// Timestep (EnzoMethodMHDVlct::timestep, EnzoMethodMHDVlct.cpp:551-588, and
+// EnzoMHDIntegratorStageCommands::timestep, .cpp:299-366).  Per cell:
+//   dual energy on: energy floor + sync (mutates etot/eint over the whole block)
+//   p from the integration quantities (written to the pressure field if given)
+//   s_d = |v_d| + c_fast  (c_fast = sqrt(B^2/rho + gamma p/rho))
+// and the kernel reduces max_cells s_d per block and axis.  Because a
+// correctly rounded division is monotone,
+//   min_cells min_d dx_d / s_d  ==  min_d dx_d / max_cells s_d
+// exactly, so the finishing kernel reproduces the reference's dt bit for bit.
+// Speeds are non-negative, so their IEEE bit patterns order like unsigned
+// integers and atomicMax on the bits is an exact max.
+// ---------------------------------------------------------------------------
+template <class R> struct SpeedBits;
+template <> struct SpeedBits<double> {
+  typedef unsigned long long T;
+  static __device__ T bits(double v) { return (T)__double_as_longlong(v); }
+  static __device__ double val(T b) { return __longlong_as_double((long long)b); }
+};
+template <> struct SpeedBits<float> {
+  typedef unsigned int T;
+  static __device__ T bits(float v) { return (T)__float_as_uint(v); }
+  static __device__ float val(T b) { return __uint_as_float(b); }
+};
+
+template <class R, bool MHD, bool DE>
+__global__ void __launch_bounds__(256)
+timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
+                int chunks_per_block, PhysParams phys,
+                typename SpeedBits<R>::T* __restrict__ smax_out) {
+  typedef typename SpeedBits<R>::T T;
+  __shared__ T red[3][8];
+  const int b = blockIdx.x / chunks_per_block;
+  const int chunk = blockIdx.x - b * chunks_per_block;
+  if (b >= nblocks) return;
+  const AuxBlock<R>& B = blocks[b];
+  const size_t ncell = (size_t)B.m[0] * B.m[1] * B.m[2];
+  const R g = R(phys.gamma);
+  R s[3] = {R(0), R(0), R(0)};
+  for (size_t c = (size_t)chunk * blockDim.x + threadIdx.x; c < ncell;
+       c += (size_t)chunks_per_block * blockDim.x) {
+    const R rho = B.f.c[F_RHO][c];
+    const R vx = B.f.c[F_VX][c], vy = B.f.c[F_VY][c], vz = B.f.c[F_VZ][c];
+    R bx = R(0), by = R(0), bz = R(0);
+    if (MHD) {
+      bx = B.f.c[F_BX][c];
+      by = B.f.c[F_BY][c];
+      bz = B.f.c[F_BZ][c];
+    }
+    R p;
+    if (DE) {
+      // apply_floor_to_energy_and_sync over the whole block (stale depth 0)
+      const double gam = phys.gamma, eta = phys.eta;
+      const float ggm1 = (float)(gam * (gam - 1.));
+      const double inv_gm1 = 1. / (gam - 1.);
+      const double half_factor = (eta != 0.) ? 0.5 : 0.;
+      const double inv_rho = 1. / (double)rho;
+      const double eint_floor = phys.pressure_floor * inv_gm1 * inv_rho;
+      const double dvx = vx, dvy = vy, dvz = vz;
+      const double v2 = (dvx * dvx + dvy * dvy + dvz * dvz);
+      double nte = 0.5 * v2, b2 = 0;
+      if (MHD) {
+        const double dbx = bx, dby = by, dbz = bz;
+        b2 = (dbx * dbx + dby * dby + dbz * dbz);
+        nte += (0.5 * b2 * inv_rho);
+      }
+      const double eint_1 = (double)B.f.c[F_ETOT][c] - nte;
+      double cur = B.f.c[F_EINT][c];
+      const double cs2_1 = fmax(0., (double)ggm1 * eint_1);
+      if ((cs2_1 > fmax(eta * v2, eta * b2 * inv_rho)) &&
+          (eint_1 > half_factor * cur))
+        cur = eint_1;
+      cur = smax(cur, eint_floor);
+      const R eint = R(cur);
+      B.f.c[F_EINT][c] = eint;
+      B.f.c[F_ETOT][c] = R(cur + nte);
+      p = R(phys.gamma - 1.0) * rho * eint;
+    } else {
+      const double dvx = vx, dvy = vy, dvz = vz;
+      const double ke = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
+      double me = 0.;
+      if (MHD) {
+        const double dbx = bx, dby = by, dbz = bz;
+        me = 0.5 * (dbx * dbx + dby * dby + dbz * dbz);
+      }
+      p = R((phys.gamma - 1.0) * ((double)rho * ((double)B.f.c[F_ETOT][c] - ke) - me));
+    }
+    if (B.pressure) B.pressure[c] = p;
+    R cf;
+    if (MHD) {  // fast_magnetosonic_speed<0> (EnzoEOSIdeal.hpp:124-126)
+      const R B2 = sqmag(bx, by, bz);
+      const R c2 = cs2(g, rho, p);
+      const R va2 = B2 / rho;
+      cf = sqrt(va2 + c2);
+    } else {
+      cf = sqrt(cs2(g, rho, p));
+    }
+    s[0] = fmax(s[0], fabs(vx) + cf);
+    s[1] = fmax(s[1], fabs(vy) + cf);
+    s[2] = fmax(s[2], fabs(vz) + cf);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    T v = SpeedBits<R>::bits(s[d]);
+    for (int o = 16; o > 0; o >>= 1) {
+      T w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = (w > v) ? w : v;
+    }
+    if (lane == 0) red[d][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int d = threadIdx.x;
+    T v = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) v = (red[d][w] > v) ? red[d][w] : v;
+    atomicMax(&smax_out[3 * b + d], v);
+  }
+}
+
+// dt_block = courant * min_d dx_d / max s_d; optionally the global minimum
+// (the Cello CkReduction::min_double, src/Cello/control_stopping.cpp:66-135)
+// is written to every block's slot.
+template <class R>
+__global__ void timestep_finish_kernel(const AuxBlock<R>* __restrict__ blocks,
+                                       int nblocks,
+                                       const typename SpeedBits<R>::T* smax_in,
+                                       double courant, int global_min,
+                                       double* dt_out, double* dt_min_out) {
+  __shared__ double red[32];
+  double local = 1.7976931348623157e308;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    const AuxBlock<R>& B = blocks[b];
+    const double sx = (double)SpeedBits<R>::val(smax_in[3 * b + 0]);
+    const double sy = (double)SpeedBits<R>::val(smax_in[3 * b + 1]);
+    const double sz = (double)SpeedBits<R>::val(smax_in[3 * b + 2]);
+    const double dt = min3(B.cw[0] / sx, B.cw[1] / sy, B.cw[2] / sz) * courant;
+    dt_out[b] = dt;
+    local = smin(local, dt);
+  }
+  for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_xor_sync(0xffffffffu, local, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = red[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = fmin(v, red[w]);
+    if (dt_min_out) *dt_min_out = v;
+    red[0] = v;
+  }
+  __syncthreads();
+  if (global_min) {
+    const double v = red[0];
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) dt_out[b] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Same-level ghost refresh (src/Cello/control_refresh.cpp:243-360,
+// data_FieldFace.cpp:439-520, mesh_Box.cpp:150-206).  For every ghost element
+// the source along each axis is: cell-centred axis, index c < g -> c + n from
+// the low neighbour, c >= g + n -> c - n from the high neighbour; face-centred
+// axis, k < g -> k + n, k > g + n -> k - n, and the block's own boundary faces
+// (k = g, g + n) are never overwritten.  nbr[27 * b + (sz+1)*9 + (sy+1)*3 +
+// (sx+1)] is the block that supplies offset (sx, sy, sz) of block b.
+// The kernel enumerates only the ghost shell of each field.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(256)
+refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ nbr,
+               int nblocks, int g, int nfield_slots, int chunks_per_block) {
+  const int b = blockIdx.x / chunks_per_block;
+  const int chunk = blockIdx.x - b * chunks_per_block;
+  if (b >= nblocks) return;
+  const AuxBlock<R>& B = blocks[b];
+  const int n[3] = {B.m[0] - 2 * g, B.m[1] - 2 * g, B.m[2] - 2 * g};
+  for (int fs = 0; fs < nfield_slots; fs++) {
+    // slots 0..8 cell fields, 9..11 face fields
+    R* dst = (fs < NCELL) ? B.f.c[fs] : B.f.f[fs - NCELL];
+    if (!dst) continue;
+    const int face = (fs < NCELL) ? -1 : fs - NCELL;
+    int e[3], lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+      e[a] = B.m[a] + (a == face);
+      lo[a] = g;
+      hi[a] = (a == face) ? g + n[a] + 1 : g + n[a];
+    }
+    const long long cz = (long long)(e[2] - (hi[2] - lo[2])) * e[1] * e[0];
+    const long long cy = (long long)(hi[2] - lo[2]) * (e[1] - (hi[1] - lo[1])) * e[0];
+    const long long cx = (long long)(hi[2] - lo[2]) * (hi[1] - lo[1]) * (e[0] - (hi[0] - lo[0]));
+    const long long total = cz + cy + cx;
+    for (long long q = (long long)chunk * blockDim.x + threadIdx.x; q < total;
+         q += (long long)chunks_per_block * blockDim.x) {
+      int x, y, z;
+      if (q < cz) {
+        const int w = e[2] - (hi[2] - lo[2]);
+        long long r = q;
+        x = (int)(r % e[0]); r /= e[0];
+        y = (int)(r % e[1]); r /= e[1];
+        const int zz = (int)r;
+        z = (zz < lo[2]) ? zz : zz + (hi[2] - lo[2]);
+        (void)w;
+      } else if (q < cz + cy) {
+        long long r = q - cz;
+        x = (int)(r % e[0]); r /= e[0];
+        const int wy = e[1] - (hi[1] - lo[1]);
+        const int yy = (int)(r % wy); r /= wy;
+        y = (yy < lo[1]) ? yy : yy + (hi[1] - lo[1]);
+        z = lo[2] + (int)r;
+      } else {
+        long long r = q - cz - cy;
+        const int wx = e[0] - (hi[0] - lo[0]);
+        const int xx = (int)(r % wx); r /= wx;
+        x = (xx < lo[0]) ? xx : xx + (hi[0] - lo[0]);
+        y = lo[1] + (int)(r % (hi[1] - lo[1])); r /= (hi[1] - lo[1]);
+        z = lo[2] + (int)r;
+      }
+      int idx[3] = {x, y, z}, src[3], side[3];
+      for (int a = 0; a < 3; a++) {
+        const int i = idx[a];
+        if (a == face) {
+          if (i < g) { side[a] = -1; src[a] = i + n[a]; }
+          else if (i > g + n[a]) { side[a] = 1; src[a] = i - n[a]; }
+          else { side[a] = 0; src[a] = i; }
+        } else {
+          if (i < g) { side[a] = -1; src[a] = i + n[a]; }
+          else if (i >= g + n[a]) { side[a] = 1; src[a] = i - n[a]; }
+          else { side[a] = 0; src[a] = i; }
+        }
+      }
+      const int sb = nbr[27 * b + (side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1)];
+      const AuxBlock<R>& SB = blocks[sb];
+      const R* sp = (fs < NCELL) ? SB.f.c[fs] : SB.f.f[fs - NCELL];
+      dst[((size_t)z * e[1] + y) * e[0] + x] = sp[((size_t)src[2] * e[1] + src[1]) * e[0] + src[0]];
+    }
+  }
+}
+
+// Copy the face-B box updated by the final stage (faces k in [lo, hi_d) along
+// d, transverse [lo, hi)) from the stage's face buffer into the caller's field.
+template <class R>
+__global__ void copy_faces_kernel(int m0, int m1, int m2, int lo_t, int S1,
+                                  const R* __restrict__ fx, const R* __restrict__ fy,
+                                  const R* __restrict__ fz, R* __restrict__ ox,
+                                  R* __restrict__ oy, R* __restrict__ oz) {
+  const int m[3] = {m0, m1, m2};
+  const R* src[3] = {fx, fy, fz};
+  R* dst[3] = {ox, oy, oz};
+  for (int d = 0; d < 3; d++) {
+    int e[3] = {m0 + (d == 0), m1 + (d == 1), m2 + (d == 2)};
+    int lo[3], cnt[3];
+    for (int a = 0; a < 3; a++) {
+      lo[a] = (a == d) ? S1 : lo_t;
+      const int hi = (a == d) ? m[a] - S1 + 1 : m[a] - lo_t;
+      cnt[a] = hi - lo[a];
+    }
+    const long long total = (long long)cnt[0] * cnt[1] * cnt[2];
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+      long long r = q;
+      const int x = lo[0] + (int)(r % cnt[0]); r /= cnt[0];
+      const int y = lo[1] + (int)(r % cnt[1]); r /= cnt[1];
+      const int z = lo[2] + (int)r;
+      const size_t i = ((size_t)z * e[1] + y) * e[0] + x;
+      dst[d][i] = src[d][i];
+    }
+  }
+}
+
+static __global__ void set_scalar_kernel(double* p, double v) { *p = v; }
+
+}  // namespace vlct

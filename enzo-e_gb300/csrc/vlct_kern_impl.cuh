@@ -1,0 +1,127 @@
+// vlct_kern_impl.cuh -- explicit instantiation and runtime dispatch of the
+// kernel templates for one precision R.  Included once per precision TU.
+#pragma once
+#include "vlct_aux.cuh"
+#include "vlct_launch.h"
+#include "vlct_stage.cuh"
+
+namespace vlct {
+
+namespace {
+template <class R, int SOLVER, int RECON, bool DE>
+cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
+                      const StageInfo& info, const PhysParams& phys, int grid,
+                      cudaStream_t st) {
+  const size_t smem = stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty);
+  auto k = stage_kernel<R, SOLVER, RECON, DE>;
+  cudaError_t e = cudaFuncSetAttribute(
+      k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (grid <= 0 || grid > nt) grid = nt;
+  if (nt <= 0) return cudaSuccess;
+  k<<<grid, 256, smem, st>>>(b, t, nt, info, phys);
+  return cudaGetLastError();
+}
+
+template <class R, int SOLVER, bool DE>
+cudaError_t stage_recon(int recon, const StageBlock<R>* b, const StageTile* t,
+                        int nt, const StageInfo& info, const PhysParams& phys,
+                        int grid, cudaStream_t st) {
+  switch (recon) {
+    case RECON_NN: return stage_one<R, SOLVER, RECON_NN, DE>(b, t, nt, info, phys, grid, st);
+    case RECON_PLM: return stage_one<R, SOLVER, RECON_PLM, DE>(b, t, nt, info, phys, grid, st);
+    case RECON_PLM_ATHENA:
+      return stage_one<R, SOLVER, RECON_PLM_ATHENA, DE>(b, t, nt, info, phys, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <class R, int SOLVER>
+cudaError_t stage_de(int recon, bool de, const StageBlock<R>* b,
+                     const StageTile* t, int nt, const StageInfo& info,
+                     const PhysParams& phys, int grid, cudaStream_t st) {
+  return de ? stage_recon<R, SOLVER, true>(recon, b, t, nt, info, phys, grid, st)
+            : stage_recon<R, SOLVER, false>(recon, b, t, nt, info, phys, grid, st);
+}
+
+template <class R, int SOLVER, bool DE>
+size_t smem_recon(int recon, int tx, int ty) {
+  switch (recon) {
+    case RECON_NN: return stage_smem_bytes<R, SOLVER, RECON_NN, DE>(tx, ty);
+    case RECON_PLM: return stage_smem_bytes<R, SOLVER, RECON_PLM, DE>(tx, ty);
+    default: return stage_smem_bytes<R, SOLVER, RECON_PLM_ATHENA, DE>(tx, ty);
+  }
+}
+}  // namespace
+
+template <>
+cudaError_t launch_stage<VLCT_REAL>(int solver, int recon, bool de,
+                                    const StageBlock<VLCT_REAL>* b,
+                                    const StageTile* t, int nt,
+                                    const StageInfo& info,
+                                    const PhysParams& phys, int grid,
+                                    cudaStream_t st) {
+  switch (solver) {
+    case SOLVER_HLLE: return stage_de<VLCT_REAL, SOLVER_HLLE>(recon, de, b, t, nt, info, phys, grid, st);
+    case SOLVER_HLLC: return stage_de<VLCT_REAL, SOLVER_HLLC>(recon, de, b, t, nt, info, phys, grid, st);
+    case SOLVER_HLLD: return stage_de<VLCT_REAL, SOLVER_HLLD>(recon, de, b, t, nt, info, phys, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <>
+size_t stage_smem<VLCT_REAL>(int solver, int recon, bool de, int tx, int ty) {
+  // the solver changes only NF (hydro vs MHD)
+  if (solver == SOLVER_HLLC) {
+    return de ? smem_recon<VLCT_REAL, SOLVER_HLLC, true>(recon, tx, ty)
+              : smem_recon<VLCT_REAL, SOLVER_HLLC, false>(recon, tx, ty);
+  }
+  return de ? smem_recon<VLCT_REAL, SOLVER_HLLD, true>(recon, tx, ty)
+            : smem_recon<VLCT_REAL, SOLVER_HLLD, false>(recon, tx, ty);
+}
+
+template <>
+cudaError_t launch_timestep<VLCT_REAL>(bool mhd, bool de,
+                                       const AuxBlock<VLCT_REAL>* b, int nb,
+                                       int cpb, const PhysParams& phys,
+                                       void* d_smax, double courant,
+                                       int global_min, double* d_dt,
+                                       double* d_dt_min, cudaStream_t st) {
+  typedef typename SpeedBits<VLCT_REAL>::T T;
+  T* smax = (T*)d_smax;
+  cudaError_t e = cudaMemsetAsync(smax, 0, sizeof(T) * 3 * (size_t)nb, st);
+  if (e != cudaSuccess) return e;
+  const int grid = nb * cpb;
+  if (mhd) {
+    if (de) timestep_kernel<VLCT_REAL, true, true><<<grid, 256, 0, st>>>(b, nb, cpb, phys, smax);
+    else timestep_kernel<VLCT_REAL, true, false><<<grid, 256, 0, st>>>(b, nb, cpb, phys, smax);
+  } else {
+    if (de) timestep_kernel<VLCT_REAL, false, true><<<grid, 256, 0, st>>>(b, nb, cpb, phys, smax);
+    else timestep_kernel<VLCT_REAL, false, false><<<grid, 256, 0, st>>>(b, nb, cpb, phys, smax);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  timestep_finish_kernel<VLCT_REAL><<<1, 256, 0, st>>>(b, nb, smax, courant, global_min,
+                                                       d_dt, d_dt_min);
+  return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_refresh<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, const int* nbr,
+                                      int nb, int g, int cpb, cudaStream_t st) {
+  refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 3, cpb);
+  return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_copy_faces<VLCT_REAL>(int m0, int m1, int m2, int S1,
+                                         const VLCT_REAL* fx, const VLCT_REAL* fy,
+                                         const VLCT_REAL* fz, VLCT_REAL* ox,
+                                         VLCT_REAL* oy, VLCT_REAL* oz,
+                                         cudaStream_t st) {
+  copy_faces_kernel<VLCT_REAL><<<256, 256, 0, st>>>(m0, m1, m2, S1, S1, fx, fy, fz,
+                                                    ox, oy, oz);
+  return cudaGetLastError();
+}
+
+}  // namespace vlct

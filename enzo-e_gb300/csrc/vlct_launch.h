@@ -1,0 +1,47 @@
+// vlct_launch.h -- typed launch entry points of the kernels (one set per
+// precision; FP64 lives in kern_f64.cu compiled with --fmad=false, FP32 in
+// kern_f32.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "vlct_types.h"
+
+namespace vlct {
+
+template <class R> struct AuxBlock;
+
+// Largest tile extent compiled for each precision.
+template <class R> struct TileLimits;
+template <> struct TileLimits<double> { static constexpr int TMAX = 16; };
+template <> struct TileLimits<float> { static constexpr int TMAX = 24; };
+
+template <class R>
+cudaError_t launch_stage(int solver, int recon, bool de,
+                         const StageBlock<R>* d_blocks, const StageTile* d_tiles,
+                         int ntiles, const StageInfo& info,
+                         const PhysParams& phys, int grid, cudaStream_t st);
+
+template <class R>
+size_t stage_smem(int solver, int recon, bool de, int tx, int ty);
+
+template <class R>
+cudaError_t launch_timestep(bool mhd, bool de, const AuxBlock<R>* d_blocks,
+                            int nblocks, int chunks_per_block,
+                            const PhysParams& phys, void* d_smax,
+                            double courant, int global_min, double* d_dt,
+                            double* d_dt_min, cudaStream_t st);
+
+template <class R>
+cudaError_t launch_refresh(const AuxBlock<R>* d_blocks, const int* d_nbr,
+                           int nblocks, int g, int chunks_per_block,
+                           cudaStream_t st);
+
+template <class R>
+cudaError_t launch_copy_faces(int m0, int m1, int m2, int S1, const R* fx,
+                              const R* fy, const R* fz, R* ox, R* oy, R* oz,
+                              cudaStream_t st);
+
+cudaError_t launch_set_scalar(double* p, double v, cudaStream_t st);
+
+}  // namespace vlct

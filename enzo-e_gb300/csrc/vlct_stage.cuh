@@ -1,0 +1,562 @@
+// vlct_stage.cuh -- one fused VL+CT stage (half or full step) for a set of
+// blocks, as a z-marching CUDA kernel.
+//
+// A CTA owns a column tile [xa, xb) x [ya, yb) of one block and marches up
+// the block's z range.  Everything between the global state read and the
+// stage's outputs stays in shared memory: the primitives of a ring of
+// z-planes, the x/y face fluxes of two planes, the z-face fluxes of two
+// faces, the cell-centred electric field, the edge EMFs and the new face B.
+// Per z-plane the CTA runs five phases separated by __syncthreads():
+//
+//   A  load primitives of plane t+L (L = 1 for NN, 2 for PLM)
+//   B  Riemann solves: z-faces at t+1/2, x- and y-faces of plane t+1;
+//      cell-centred E of plane t+1
+//   C  upwinded edge EMFs: E_x, E_y at t+1/2 and E_z of plane t
+//   D1 constrained-transport face updates: Bz at t+1/2, Bx / By of plane t
+//   D2 cell updates of plane t: centred B, flux divergence + dual-energy
+//      source, density floor, energy floor / dual-energy sync; store.
+//
+// The index windows of every quantity are those of the reference's array
+// passes (EnzoMHDIntegratorStageCommands::compute_update_stage,
+// src/Enzo/hydro-mhd/EnzoMHDIntegratorStageCommands.cpp:102-261, with the
+// stale-depth bookkeeping of EnzoMethodMHDVlct::compute, :459-496), so the
+// values written are the reference's values wherever the reference defines
+// them.  The FP64 instantiation is compiled with --fmad=false and matches the
+// reference bit for bit; in the FP32 instantiation the pressure recovery
+// (total minus kinetic minus magnetic energy) and the energy floor / sync run
+// in FP64.
+#pragma once
+#include "vlct_physics.cuh"
+#include "vlct_types.h"
+
+namespace vlct {
+
+// global primitive slot order: rho, Bx, By, Bz, vx, vy, vz, p
+enum { Q_RHO = 0, Q_BX = 1, Q_VX = 4, Q_P = 7, NQ = 8 };
+// shared flux slots: rho, mom x/y/z, etot, B_(d+1), B_(d+2), eint, vbar
+enum { S_RHO = 0, S_MX = 1, S_E = 4, S_BJ = 5, S_BK = 6, S_EINT = 7, S_VBAR = 8 };
+
+__device__ __forceinline__ bool inr(int a, int lo, int hi) {
+  return a >= lo && a < hi;
+}
+
+// Upwind weight of CT from the sign of the density flux
+// (EnzoBfieldMethodCT.cpp:198-213).
+template <class R> __device__ __forceinline__ R upw(R fd) {
+  return (fd > R(0)) ? R(1.0) : ((fd < R(0)) ? R(0.0) : R(0.5));
+}
+
+// compute_edge_<true> (EnzoBfieldMethodCT.cpp:384-457)
+template <class R>
+__device__ __forceinline__ R edge_emf(R Ej, R Ej_kp1, R Ek, R Ek_jp1, R Wj,
+                                      R Wj_kp1, R Wk, R Wk_jp1, R Ec, R Ec_jp1,
+                                      R Ec_kp1, R Ec_jkp1) {
+  R dEdj_r = Wk_jp1 * (Ec_jp1 + Ej) + (R(1) - Wk_jp1) * (Ec_jkp1 + Ej_kp1);
+  R dEdj_l = Wk * (-Ej - Ec) + (R(1) - Wk) * (-Ej_kp1 - Ec_kp1);
+  R dEdk_r = Wj_kp1 * (Ec_kp1 - Ek) + (R(1) - Wj_kp1) * (Ec_jkp1 - Ek_jp1);
+  R dEdk_l = Wj * (Ek - Ec) + (R(1) - Wj) * (Ek_jp1 - Ec_jp1);
+  R Ej_sum = Ej + Ej_kp1;
+  Ej_sum *= R(-1);
+  R Ek_sum = Ek + Ek_jp1;
+  return R(0.25) * (Ej_sum + Ek_sum + (dEdj_l - dEdj_r) + (dEdk_l - dEdk_r));
+}
+
+template <class R, int SOLVER, int RECON, bool DE> struct StageCfg {
+  static constexpr bool MHD = SOLVER != SOLVER_HLLC;
+  static constexpr int LOOK = (RECON == RECON_NN) ? 1 : 2;
+  static constexpr int NRING = 2 * LOOK;
+  static constexpr int RP = (RECON == RECON_NN) ? 0 : 1;
+  static constexpr int NF = DE ? 9 : (MHD ? 7 : 5);
+};
+
+// Shared-memory carve-up for a launch whose tiles are at most tx x ty.
+struct SmemLayout {
+  int PP, QP;   // primitive tile pitch / rows
+  int HP, HQ;   // halo grid pitch / rows (tile + 1 cell each side)
+  int G;        // HP * HQ
+  int o_prim, o_xf, o_yf, o_zf, o_ec, o_ex, o_ey, o_ez, o_bx, o_by, o_bz;
+  int total;    // in elements of R
+  __host__ __device__ void init(int tx, int ty, int rp, int nring, int nf) {
+    PP = tx + 2 + 2 * rp;
+    QP = ty + 2 + 2 * rp;
+    HP = tx + 2;
+    HQ = ty + 2;
+    G = HP * HQ;
+    int o = 0;
+    o_prim = o; o += nring * NQ * PP * QP;
+    o_xf = o; o += 2 * nf * G;
+    o_yf = o; o += 2 * nf * G;
+    o_zf = o; o += 2 * nf * G;
+    o_ec = o; o += 2 * 3 * G;
+    o_ex = o; o += 2 * G;
+    o_ey = o; o += 2 * G;
+    o_ez = o; o += G;
+    o_bx = o; o += G;
+    o_by = o; o += G;
+    o_bz = o; o += 2 * G;
+    total = o;
+  }
+};
+
+template <class R, int SOLVER, int RECON, bool DE>
+size_t stage_smem_bytes(int tx, int ty) {
+  using C = StageCfg<R, SOLVER, RECON, DE>;
+  SmemLayout L;
+  L.init(tx, ty, C::RP, C::NRING, C::NF);
+  return (size_t)L.total * sizeof(R);
+}
+
+template <class R, int SOLVER, int RECON, bool DE>
+__global__ void __launch_bounds__(256)
+stage_kernel(const StageBlock<R>* __restrict__ blocks,
+             const StageTile* __restrict__ tiles, int ntiles, StageInfo info,
+             PhysParams phys) {
+  using C = StageCfg<R, SOLVER, RECON, DE>;
+  constexpr bool MHD = C::MHD;
+  constexpr int LOOK = C::LOOK, NRING = C::NRING, RP = C::RP, NF = C::NF;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* sm = reinterpret_cast<R*>(smem_raw);
+  SmemLayout Ls;
+  Ls.init(info.tx, info.ty, RP, NRING, NF);
+  const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;
+  R* s_prim = sm + Ls.o_prim;
+  R* s_xf = sm + Ls.o_xf;
+  R* s_yf = sm + Ls.o_yf;
+  R* s_zf = sm + Ls.o_zf;
+  R* s_ec = sm + Ls.o_ec;
+  R* s_ex = sm + Ls.o_ex;
+  R* s_ey = sm + Ls.o_ey;
+  R* s_ez = sm + Ls.o_ez;
+  R* s_bx = sm + Ls.o_bx;
+  R* s_by = sm + Ls.o_by;
+  R* s_bz = sm + Ls.o_bz;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int s = info.s, S = info.S;
+  const R g = R(phys.gamma);
+  const R theta = R(phys.theta_limiter);
+  const R dfloor = R(phys.density_floor), pfloor = R(phys.pressure_floor);
+
+  for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
+    const StageTile tl = tiles[it];
+    const StageBlock<R>& B = blocks[tl.block];
+    const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
+    const int xa = tl.xa, xb = tl.xb, ya = tl.ya, yb = tl.yb;
+    const int tx = xb - xa, ty = yb - ya;
+    const double dt = *B.dt * info.dt_factor;
+    const R dtdx[3] = {R(dt / B.cw[0]), R(dt / B.cw[1]), R(dt / B.cw[2])};
+    // output window of centred B (and the z-march range)
+    const int olo = info.final_stage ? S : S + 1;
+    const int ohi_x = info.final_stage ? m0 - S : m0 - S - 1;
+    const int ohi_y = info.final_stage ? m1 - S : m1 - S - 1;
+    const int ohi_z = info.final_stage ? m2 - S : m2 - S - 1;
+    const int za = tl.za, zb = tl.zb;  // output planes of this chunk
+    const int t0 = za - 1;
+    // prim-tile origin and halo-grid origin
+    const int px0 = xa - 1 - RP, py0 = ya - 1 - RP;
+    const int hx0 = xa - 1, hy0 = ya - 1;
+    const size_t cstr_y = (size_t)m0, cstr_z = (size_t)m0 * m1;
+
+    auto prim_at = [&](int slot, int q, int x, int y) -> R& {
+      return s_prim[((slot * NQ + q) * QP + (y - py0)) * PP + (x - px0)];
+    };
+
+    // ---- phase A: primitives of plane p into ring slot p % NRING --------
+    auto load_plane = [&](int p) {
+      if (!inr(p, s, m2 - s)) return;
+      const int slot = p % NRING;
+      const double gm1 = phys.gamma - 1.0;
+      for (int idx = tid; idx < PP * QP; idx += nthr) {
+        const int x = px0 + idx % PP, y = py0 + idx / PP;
+        if (!inr(x, s, m0 - s) || !inr(y, s, m1 - s)) continue;
+        const size_t c = (size_t)p * cstr_z + (size_t)y * cstr_y + x;
+        const R rho = B.cur.c[F_RHO][c];
+        const R vx = B.cur.c[F_VX][c], vy = B.cur.c[F_VY][c], vz = B.cur.c[F_VZ][c];
+        R bx = R(0), by = R(0), bz = R(0);
+        if (MHD) {
+          bx = B.cur.c[F_BX][c];
+          by = B.cur.c[F_BY][c];
+          bz = B.cur.c[F_BZ][c];
+        }
+        R p_out;
+        // EnzoComputePressure::compute_pressure (EnzoComputePressure.cpp:127-190)
+        if (DE) {
+          p_out = R(gm1) * rho * B.cur.c[F_EINT][c];
+        } else {
+          // total minus kinetic minus magnetic energy: FP64 in both forms
+          const double dvx = vx, dvy = vy, dvz = vz;
+          const double ke = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
+          double me = 0.;
+          if (MHD) {
+            const double dbx = bx, dby = by, dbz = bz;
+            me = 0.5 * (dbx * dbx + dby * dby + dbz * dbz);
+          }
+          p_out = R(gm1 * ((double)rho * ((double)B.cur.c[F_ETOT][c] - ke) - me));
+        }
+        prim_at(slot, Q_RHO, x, y) = rho;
+        prim_at(slot, Q_VX + 0, x, y) = vx;
+        prim_at(slot, Q_VX + 1, x, y) = vy;
+        prim_at(slot, Q_VX + 2, x, y) = vz;
+        if (MHD) {
+          prim_at(slot, Q_BX + 0, x, y) = bx;
+          prim_at(slot, Q_BX + 1, x, y) = by;
+          prim_at(slot, Q_BX + 2, x, y) = bz;
+        }
+        prim_at(slot, Q_P, x, y) = p_out;
+      }
+    };
+
+    // Reconstructed L/R primitives of one face (face frame) along dim d.
+    // w(k) returns the primitive q at the k-th cell along d (k = -1..2 around
+    // the face between cells 0 and 1).
+    auto reconstruct = [&](int d, auto&& w, R* wl, R* wr) {
+      const int qmap[8] = {Q_RHO, Q_BX + d, Q_BX + (d + 1) % 3, Q_BX + (d + 2) % 3,
+                           Q_VX + d, Q_VX + (d + 1) % 3, Q_VX + (d + 2) % 3, Q_P};
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        if (!MHD && (k == L_BI || k == L_BJ || k == L_BK)) {
+          wl[k] = wr[k] = R(0);
+          continue;
+        }
+        const int q = qmap[k];
+        if (RECON == RECON_NN) {
+          wl[k] = w(q, 0);
+          wr[k] = w(q, 1);
+        } else {
+          const R a = w(q, -1), b0 = w(q, 0), b1 = w(q, 1), c = w(q, 2);
+          R dl, dr;
+          if (RECON == RECON_PLM) {
+            dl = limiter_enzo_rk(a, b0, b1, theta);
+            dr = limiter_enzo_rk(b0, b1, c, theta);
+          } else {
+            dl = limiter_athena(a, b0, b1);
+            dr = limiter_athena(b0, b1, c);
+          }
+          const R hl = dl * R(0.5), hr = dr * R(0.5);
+          R lv = b0 + hl, rv = b1 - hr;
+          if (q == Q_RHO) {
+            lv = smax(lv, dfloor);
+            rv = smax(rv, dfloor);
+          } else if (q == Q_P) {
+            lv = smax(lv, pfloor);
+            rv = smax(rv, pfloor);
+          }
+          wl[k] = lv;
+          wr[k] = rv;
+        }
+      }
+    };
+
+    // Solve one face and store its fluxes (global component order).
+    auto solve_store = [&](int d, R* wl, R* wr, R* dst) {
+      FaceFlux<R> F;
+      riemann<SOLVER, R>(g, wl, wr, F);
+      dst[S_RHO * G] = F.f[L_RHO];
+      dst[(S_MX + d) * G] = F.f[L_VI];
+      dst[(S_MX + (d + 1) % 3) * G] = F.f[L_VJ];
+      dst[(S_MX + (d + 2) % 3) * G] = F.f[L_VK];
+      dst[S_E * G] = F.f[L_E];
+      if (MHD) {
+        dst[S_BJ * G] = F.f[L_BJ];
+        dst[S_BK * G] = F.f[L_BK];
+      }
+      if (DE) {
+        dst[S_EINT * G] = F.eflux;
+        dst[S_VBAR * G] = F.vbar;
+      }
+    };
+
+    // ---- phase B items for step t: z-faces at t+1/2, x/y faces and
+    // cell-centred E of plane t+1 (the prologue runs the plane part only).
+    auto phase_b = [&](int t, bool zfaces, int pl) {
+      const bool plane_ok = inr(pl, S, m2 - S);
+      const int nitem = 4 * G;
+      for (int idx = tid; idx < nitem; idx += nthr) {
+        const int kind = idx / G, r = idx - kind * G;
+        const int i = r % HP, j = r / HP;
+        const int x = hx0 + i, y = hy0 + j;
+        R wl[8], wr[8];
+        if (kind == 0) {  // z-face fz = t (between planes t and t+1)
+          const int fz = t;
+          if (!zfaces || !inr(fz, S, m2 - 1 - S) || !inr(x, S, m0 - S) ||
+              !inr(y, S, m1 - S))
+            continue;
+          reconstruct(2, [&](int q, int k) -> R {
+            return prim_at((fz + k + NRING) % NRING, q, x, y);
+          }, wl, wr);
+          if (MHD) {  // correct_reconstructed_bfield (EnzoBfieldMethodCT.cpp:122-166)
+            const R bf = B.cur.f[2][(size_t)(fz + 1) * cstr_z + (size_t)y * cstr_y + x];
+            wl[L_BI] = bf;
+            wr[L_BI] = bf;
+          }
+          solve_store(2, wl, wr, s_zf + (size_t)(fz & 1) * NF * G + r);
+        } else if (kind == 1) {  // x-face fx = x of plane pl
+          if (i > tx || !plane_ok || !inr(x, S, m0 - 1 - S) || !inr(y, S, m1 - S))
+            continue;
+          const int slot = pl % NRING;
+          reconstruct(0, [&](int q, int k) -> R { return prim_at(slot, q, x + k, y); },
+                      wl, wr);
+          if (MHD) {
+            const R bf = B.cur.f[0][(size_t)pl * (m1 * (size_t)(m0 + 1)) +
+                                    (size_t)y * (m0 + 1) + (x + 1)];
+            wl[L_BI] = bf;
+            wr[L_BI] = bf;
+          }
+          solve_store(0, wl, wr, s_xf + (size_t)(pl & 1) * NF * G + r);
+        } else if (kind == 2) {  // y-face fy = y of plane pl
+          if (j > ty || !plane_ok || !inr(y, S, m1 - 1 - S) || !inr(x, S, m0 - S))
+            continue;
+          const int slot = pl % NRING;
+          reconstruct(1, [&](int q, int k) -> R { return prim_at(slot, q, x, y + k); },
+                      wl, wr);
+          if (MHD) {
+            const R bf = B.cur.f[1][(size_t)pl * ((size_t)(m1 + 1) * m0) +
+                                    (size_t)(y + 1) * m0 + x];
+            wl[L_BI] = bf;
+            wr[L_BI] = bf;
+          }
+          solve_store(1, wl, wr, s_yf + (size_t)(pl & 1) * NF * G + r);
+        } else {  // cell-centred E (EnzoBfieldMethodCT.cpp:267-292)
+          if (!MHD || !plane_ok || !inr(x, S, m0 - S) || !inr(y, S, m1 - S)) continue;
+          const int slot = pl % NRING;
+          const R vx = prim_at(slot, Q_VX, x, y), vy = prim_at(slot, Q_VX + 1, x, y),
+                  vz = prim_at(slot, Q_VX + 2, x, y);
+          const R bx = prim_at(slot, Q_BX, x, y), by = prim_at(slot, Q_BX + 1, x, y),
+                  bz = prim_at(slot, Q_BX + 2, x, y);
+          R* e = s_ec + (size_t)(pl & 1) * 3 * G + r;
+          e[0] = (-vy * bz + vz * by);
+          e[G] = (-vz * bx + vx * bz);
+          e[2 * G] = (-vx * by + vy * bx);
+        }
+      }
+    };
+
+    // ---------------------------------------------------------- prologue --
+    for (int p = t0 - (LOOK - 1); p <= t0 + LOOK - 1; p++) load_plane(p);
+    __syncthreads();
+    phase_b(t0 - 1, false, t0);
+    __syncthreads();
+
+    for (int t = t0; t < zb; t++) {
+      // ---- A
+      load_plane(t + LOOK);
+      __syncthreads();
+      // ---- B
+      phase_b(t, true, t + 1);
+      __syncthreads();
+      // ---- C: edge EMFs (EnzoBfieldMethodCT.cpp:480-590)
+      if (MHD) {
+        const R* xf0 = s_xf + (size_t)(t & 1) * NF * G;
+        const R* xf1 = s_xf + (size_t)((t + 1) & 1) * NF * G;
+        const R* yf0 = s_yf + (size_t)(t & 1) * NF * G;
+        const R* yf1 = s_yf + (size_t)((t + 1) & 1) * NF * G;
+        const R* zf = s_zf + (size_t)(t & 1) * NF * G;
+        const R* ec0 = s_ec + (size_t)(t & 1) * 3 * G;
+        const R* ec1 = s_ec + (size_t)((t + 1) & 1) * 3 * G;
+        for (int idx = tid; idx < 3 * G; idx += nthr) {
+          const int kind = idx / G, r = idx - kind * G;
+          const int i = r % HP, j = r / HP;
+          const int x = hx0 + i, y = hy0 + j;
+          if (kind == 0) {  // E_x at (x, y+1/2, t+1/2)
+            if (i < 1 || i > tx || j > ty) continue;
+            if (!inr(x, S + 1, m0 - S - 1) || !inr(y, S, m1 - S - 1) ||
+                !inr(t, S, m2 - S - 1))
+              continue;
+            s_ex[(t & 1) * G + r] = edge_emf<R>(
+                yf0[S_BJ * G + r], yf1[S_BJ * G + r], zf[S_BK * G + r],
+                zf[S_BK * G + r + HP], upw(yf0[r]), upw(yf1[r]), upw(zf[r]),
+                upw(zf[r + HP]), ec0[r], ec0[r + HP], ec1[r], ec1[r + HP]);
+          } else if (kind == 1) {  // E_y at (x+1/2, y, t+1/2)
+            if (i > tx || j < 1 || j > ty) continue;
+            if (!inr(x, S, m0 - S - 1) || !inr(y, S + 1, m1 - S - 1) ||
+                !inr(t, S, m2 - S - 1))
+              continue;
+            s_ey[(t & 1) * G + r] = edge_emf<R>(
+                zf[S_BJ * G + r], zf[S_BJ * G + r + 1], xf0[S_BK * G + r],
+                xf1[S_BK * G + r], upw(zf[r]), upw(zf[r + 1]), upw(xf0[r]),
+                upw(xf1[r]), ec0[G + r], ec1[G + r], ec0[G + r + 1],
+                ec1[G + r + 1]);
+          } else {  // E_z at (x+1/2, y+1/2, t)
+            if (i > tx || j > ty) continue;
+            if (!inr(x, S, m0 - S - 1) || !inr(y, S, m1 - S - 1) ||
+                !inr(t, S + 1, m2 - S - 1))
+              continue;
+            s_ez[r] = edge_emf<R>(
+                xf0[S_BJ * G + r], xf0[S_BJ * G + r + HP], yf0[S_BK * G + r],
+                yf0[S_BK * G + r + 1], upw(xf0[r]), upw(xf0[r + HP]),
+                upw(yf0[r]), upw(yf0[r + 1]), ec0[2 * G + r],
+                ec0[2 * G + r + 1], ec0[2 * G + r + HP], ec0[2 * G + r + HP + 1]);
+          }
+        }
+        __syncthreads();
+        // ---- D1: face updates (EnzoBfieldMethodCT.cpp:617-687); a face that
+        // is not updated in this stage keeps its start-of-step value.
+        const bool do_plane = t >= za;
+        // the lowest face of a chunk is written by the chunk below it
+        const bool own_bz = t >= za || za == olo;
+        for (int idx = tid; idx < 3 * G; idx += nthr) {
+          const int kind = idx / G, r = idx - kind * G;
+          const int i = r % HP, j = r / HP;
+          const int x = hx0 + i, y = hy0 + j;
+          if (kind == 0) {  // Bz at face kz = t+1 of column (x, y)
+            if (i < 1 || i > tx || j < 1 || j > ty) continue;
+            const int kz = t + 1;
+            if (kz > m2) continue;
+            const size_t fi = (size_t)kz * cstr_z + (size_t)y * cstr_y + x;
+            const bool upd = inr(kz, S + 1, m2 - S) && inr(x, S + 1, m0 - S - 1) &&
+                             inr(y, S + 1, m1 - S - 1);
+            R v;
+            if (upd) {
+              const R Ek_term = dtdx[0] * (s_ey[(t & 1) * G + r] - s_ey[(t & 1) * G + r - 1]);
+              const R Ej_term = dtdx[1] * (s_ex[(t & 1) * G + r] - s_ex[(t & 1) * G + r - HP]);
+              v = B.base.f[2][fi] - Ek_term + Ej_term;
+              if (own_bz) B.out.f[2][fi] = v;
+            } else {
+              v = B.base.f[2][fi];
+            }
+            s_bz[(kz & 1) * G + r] = v;
+          } else if (kind == 1) {  // Bx at face kx = x of plane t
+            if (!do_plane || i < 1 || i > tx + 1 || j < 1 || j > ty) continue;
+            const int kx = x;
+            const size_t fi = (size_t)t * ((size_t)m1 * (m0 + 1)) + (size_t)y * (m0 + 1) + kx;
+            const bool upd = inr(kx, S + 1, m0 - S) && inr(y, S + 1, m1 - S - 1) &&
+                             inr(t, S + 1, m2 - S - 1);
+            R v;
+            if (upd) {
+              // E_z at (kx-1/2, y -+ 1/2), E_y at (kx-1/2, t -+ 1/2)
+              const int re = r - 1;  // edge ex = kx - 1
+              const R Ek_term = dtdx[1] * (s_ez[re] - s_ez[re - HP]);
+              const R Ej_term = dtdx[2] * (s_ey[(t & 1) * G + re] - s_ey[((t - 1) & 1) * G + re]);
+              v = B.base.f[0][fi] - Ek_term + Ej_term;
+              if (kx < xb || (kx == xb && xb == ohi_x)) B.out.f[0][fi] = v;
+            } else {
+              v = B.base.f[0][fi];
+            }
+            s_bx[r] = v;
+          } else {  // By at face ky = y of plane t
+            if (!do_plane || i < 1 || i > tx || j < 1 || j > ty + 1) continue;
+            const int ky = y;
+            const size_t fi = (size_t)t * ((size_t)(m1 + 1) * m0) + (size_t)ky * m0 + x;
+            const bool upd = inr(ky, S + 1, m1 - S) && inr(x, S + 1, m0 - S - 1) &&
+                             inr(t, S + 1, m2 - S - 1);
+            R v;
+            if (upd) {
+              // E_x at (x, ky-1/2, t -+ 1/2), E_z at (x -+ 1/2, ky-1/2)
+              const int re = r - HP;  // edge ey = ky - 1
+              const R Ek_term = dtdx[2] * (s_ex[(t & 1) * G + re] - s_ex[((t - 1) & 1) * G + re]);
+              const R Ej_term = dtdx[0] * (s_ez[re] - s_ez[re - 1]);
+              v = B.base.f[1][fi] - Ek_term + Ej_term;
+              if (ky < yb || (ky == yb && yb == ohi_y)) B.out.f[1][fi] = v;
+            } else {
+              v = B.base.f[1][fi];
+            }
+            s_by[r] = v;
+          }
+        }
+      }
+      __syncthreads();
+      // ---- D2: cell updates of plane t
+      if (t >= za) {
+        const R* xf0 = s_xf + (size_t)(t & 1) * NF * G;
+        const R* yf0 = s_yf + (size_t)(t & 1) * NF * G;
+        const R* zfm = s_zf + (size_t)((t - 1) & 1) * NF * G;
+        const R* zfp = s_zf + (size_t)(t & 1) * NF * G;
+        const int slot = t % NRING;
+        for (int idx = tid; idx < tx * ty; idx += nthr) {
+          const int x = xa + idx % tx, y = ya + idx / tx;
+          const int r = (y - hy0) * HP + (x - hx0);
+          const size_t c = (size_t)t * cstr_z + (size_t)y * cstr_y + x;
+          const bool in_out = x < ohi_x && y < ohi_y;
+          if (!in_out) continue;
+          R bcx = R(0), bcy = R(0), bcz = R(0);
+          if (MHD) {  // compute_center_bfield (EnzoBfieldMethodCT.cpp:702-728)
+            bcx = R(0.5) * (s_bx[r] + s_bx[r + 1]);
+            bcy = R(0.5) * (s_by[r] + s_by[r + HP]);
+            bcz = R(0.5) * (s_bz[(t & 1) * G + r] + s_bz[((t + 1) & 1) * G + r]);
+            B.out.c[F_BX][c] = bcx;
+            B.out.c[F_BY][c] = bcy;
+            B.out.c[F_BZ][c] = bcz;
+          }
+          if (!inr(x, S + 1, m0 - S - 1) || !inr(y, S + 1, m1 - S - 1) ||
+              !inr(t, S + 1, m2 - S - 1))
+            continue;
+          // flux divergence, x then y then z
+          // (EnzoIntegrationQuanUpdate.cpp:105-147, EnzoSourceInternalEnergy.cpp:16-92)
+          R du[6];
+#pragma unroll
+          for (int k = 0; k < 5; k++) {
+            R a = R(0.0);
+            a -= dtdx[0] * (xf0[k * G + r] - xf0[k * G + r - 1]);
+            a -= dtdx[1] * (yf0[k * G + r] - yf0[k * G + r - HP]);
+            a -= dtdx[2] * (zfp[k * G + r] - zfm[k * G + r]);
+            du[k] = a;
+          }
+          if (DE) {
+            const R p = smax(prim_at(slot, Q_P, x, y), pfloor);
+            R a = R(0.0);
+            a -= dtdx[0] * (xf0[S_EINT * G + r] - xf0[S_EINT * G + r - 1]);
+            a -= dtdx[0] * p * (xf0[S_VBAR * G + r] - xf0[S_VBAR * G + r - 1]);
+            a -= dtdx[1] * (yf0[S_EINT * G + r] - yf0[S_EINT * G + r - HP]);
+            a -= dtdx[1] * p * (yf0[S_VBAR * G + r] - yf0[S_VBAR * G + r - HP]);
+            a -= dtdx[2] * (zfp[S_EINT * G + r] - zfm[S_EINT * G + r]);
+            a -= dtdx[2] * p * (zfp[S_VBAR * G + r] - zfm[S_VBAR * G + r]);
+            du[5] = a;
+          }
+          // update_quantities (EnzoIntegrationQuanUpdate.cpp:183-231)
+          const R old_rho = B.base.c[F_RHO][c];
+          R new_rho = old_rho + du[0];
+          new_rho = smax(new_rho, dfloor);
+          const R inv_new_rho = R(1.) / new_rho;
+          R vx = (B.base.c[F_VX][c] * old_rho + du[1]) * inv_new_rho;
+          R vy = (B.base.c[F_VY][c] * old_rho + du[2]) * inv_new_rho;
+          R vz = (B.base.c[F_VZ][c] * old_rho + du[3]) * inv_new_rho;
+          R etot = (B.base.c[F_ETOT][c] * old_rho + du[4]) * inv_new_rho;
+          R eint = R(0);
+          if (DE) eint = (B.base.c[F_EINT][c] * old_rho + du[5]) * inv_new_rho;
+          // apply_floor_to_energy_and_sync (EnzoPhysicsFluidProps.cpp:162-290),
+          // evaluated in FP64
+          {
+            const double gam = phys.gamma;
+            const double eta = DE ? phys.eta : 0.0;
+            const float ggm1 = (float)(gam * (gam - 1.));
+            const double inv_gm1 = 1. / (gam - 1.);
+            const double half_factor = (eta != 0.) ? 0.5 : 0.;
+            const double inv_rho = 1. / (double)new_rho;
+            const double eint_floor = phys.pressure_floor * inv_gm1 * inv_rho;
+            const double dvx = vx, dvy = vy, dvz = vz;
+            const double v2 = (dvx * dvx + dvy * dvy + dvz * dvz);
+            double nte = 0.5 * v2;
+            double b2 = 0;
+            if (MHD) {
+              const double dbx = bcx, dby = bcy, dbz = bcz;
+              b2 = (dbx * dbx + dby * dby + dbz * dbz);
+              nte += (0.5 * b2 * inv_rho);
+            }
+            if (DE) {
+              const double eint_1 = (double)etot - nte;
+              double cur = eint;
+              const double cs2_1 = fmax(0., (double)ggm1 * eint_1);
+              if ((cs2_1 > fmax(eta * v2, eta * b2 * inv_rho)) &&
+                  (eint_1 > half_factor * cur))
+                cur = eint_1;
+              cur = smax(cur, eint_floor);
+              eint = R(cur);
+              etot = R(cur + nte);
+            } else {
+              const double etot_floor = eint_floor + nte;
+              etot = R(smax((double)etot, etot_floor));
+            }
+          }
+          B.out.c[F_RHO][c] = new_rho;
+          B.out.c[F_VX][c] = vx;
+          B.out.c[F_VY][c] = vy;
+          B.out.c[F_VZ][c] = vz;
+          B.out.c[F_ETOT][c] = etot;
+          if (DE) B.out.c[F_EINT][c] = eint;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace vlct

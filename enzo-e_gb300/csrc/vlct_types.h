@@ -1,0 +1,54 @@
+// vlct_types.h -- host/device descriptors shared by the kernels and the C ABI.
+#pragma once
+#include <stdint.h>
+
+namespace vlct {
+
+// Cell-centred integration quantities of one block, in Cello's layout
+// (src/Cello/data_FieldData.cpp:585-619): (z, y, x), x fastest, ghosted
+// extent m = n + 2g per axis.  Face field d has extent m_d + 1 along d.
+enum CellField {
+  F_RHO = 0, F_VX, F_VY, F_VZ, F_ETOT, F_EINT, F_BX, F_BY, F_BZ, NCELL
+};
+
+template <class R> struct FieldSet {
+  R* c[NCELL];  // cell fields (F_EINT / F_B* may be null)
+  R* f[3];      // face-centred B (null in hydro mode)
+};
+
+// One block as seen by a stage kernel.
+template <class R> struct StageBlock {
+  int m[3];              // ghosted extents along x, y, z
+  double cw[3];          // cell widths
+  const double* dt;      // device pointer to this block's full step dt
+  FieldSet<R> cur;       // state the fluxes are computed from
+  FieldSet<R> base;      // start-of-step state (U^n, face B^n)
+  FieldSet<R> out;       // where the stage writes (out.f = new face B)
+};
+
+// One unit of work: a column tile [xa, xb) x [ya, yb) of one block, whose
+// output planes are [za, zb) (a z-chunk; za/zb span the whole output range
+// when the block is not chunked).
+struct StageTile {
+  int block;
+  int xa, xb, ya, yb, za, zb;
+};
+
+struct PhysParams {
+  double gamma;
+  double density_floor;
+  double pressure_floor;
+  double theta_limiter;
+  double eta;
+};
+
+// Per-stage scalars.
+struct StageInfo {
+  int s;            // stale depth at stage start
+  int S;            // stale depth after reconstruction (s + immediate rate)
+  int final_stage;  // 1 on the last stage (writes layer S of centred B)
+  double dt_factor; // 0.5 for the half step, 1 for the full step
+  int tx, ty;       // maximum tile extent of the launch (sizes shared memory)
+};
+
+}  // namespace vlct

@@ -1,0 +1,204 @@
+/*
+ * mhdvlct_gb300.h -- C ABI of the GB300 VL+CT magnetohydrodynamics step.
+ *
+ * Drop-in for Enzo-E's Method "mhd_vlct" (src/Enzo/hydro-mhd/
+ * EnzoMethodMHDVlct.{hpp,cpp}).  The Cello plugin boundary is the Method
+ * interface (src/Cello/problem_Method.hpp:23-124): compute(Block*) and
+ * timestep(Block*).  This header exposes the same two operations on one
+ * ghosted block held in device memory in Cello's layout, plus the ghost
+ * refresh that Cello performs between them, a batched form over many blocks
+ * and a serving loop over independent solves.
+ *
+ * Conventions
+ *  - Every function returns 0 on success and a positive MHD_ERR_* code on
+ *    failure; none aborts.  mhdvlct_last_error_string() describes the last
+ *    failure of a handle.
+ *  - Field arrays follow Cello's FieldData layout
+ *    (src/Cello/data_FieldData.cpp:585-619): row-major (z, y, x), x fastest,
+ *    extent n + 2g per axis, no padding; the face-centred field bfieldi_d has
+ *    one extra entry along axis d.
+ *  - Block-level device memory is caller-owned; batch and serving memory is
+ *    library-owned.  One handle per host thread.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy stream).
+ */
+#ifndef MHDVLCT_GB300_H
+#define MHDVLCT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- errors */
+enum {
+  MHD_OK = 0,
+  MHD_ERR_INVALID = 1,     /* bad argument or unsupported combination      */
+  MHD_ERR_CUDA = 2,        /* a CUDA call failed                           */
+  MHD_ERR_NOMEM = 3,       /* device allocation failed / over budget       */
+  MHD_ERR_GHOST = 4,       /* ghost depth too small for the stages         */
+  MHD_ERR_NONFINITE = 5,   /* a non-finite value was detected              */
+  MHD_ERR_TIMEOUT = 6,     /* a bounded wait ran out                       */
+  MHD_ERR_BUSY = 7         /* request not finished / queue full            */
+};
+
+enum { MHD_DTYPE_F64 = 0, MHD_DTYPE_F32 = 1 };
+
+/* -------------------------------------------------------------- params
+ * The Method:mhd_vlct parameter block and the fluid properties it uses
+ * (EnzoMethodMHDVlct.cpp:39-101; Physics:fluid_props in
+ * src/Enzo/enzo-core/EnzoConfig.cpp:952-1262).  Defaults as in the
+ * reference: riemann_solver "hlld", time_scheme "vl", reconstruct_method
+ * "plm", theta_limiter 1.5, courant 0.3 (vl), gamma 5/3, dual-energy eta
+ * 0.001.  mhd_choice has no default (the reference ERRORs when it is unset). */
+typedef struct MhdVlctParams {
+  char mhd_choice[32];          /* "constrained_transport" | "no_bfield"      */
+  char riemann_solver[16];      /* "hlle" | "hllc" | "hlld"                   */
+  char time_scheme[16];         /* "vl" | "euler"                             */
+  char reconstruct_method[16];  /* "nn" | "plm" | "plm_enzo" | "plm_athena"   */
+  double theta_limiter;
+  double courant;
+  double gamma;
+  double density_floor;
+  double pressure_floor;
+  int dual_energy;              /* 0: disabled, 1: "modern" formulation       */
+  double dual_energy_eta;
+} MhdVlctParams;
+
+/* Fill with the reference defaults (mhd_choice left empty). */
+void mhdvlct_params_default(MhdVlctParams* p);
+
+/* Parse a Cello-style parameter text such as
+ *   Method { mhd_vlct { mhd_choice = "constrained_transport";
+ *                       riemann_solver = "hlld"; courant = 0.4; }; }
+ *   Physics { fluid_props { eos { gamma = 1.6666666666666667; }
+ *             floors { density = 1e-200; pressure = 1e-200; }
+ *             dual_energy { type = "modern"; eta = 0.001; } } }
+ * Only the keys of this path are read; others are ignored.  Returns
+ * MHD_ERR_INVALID with a message in errbuf on a malformed value. */
+int mhdvlct_params_parse(const char* text, MhdVlctParams* out, char* errbuf,
+                         size_t errbuf_len);
+
+/* --------------------------------------------------------------- handle */
+typedef struct mhdvlct_handle mhdvlct_handle;
+
+/* EnzoMethodMHDVlct::EnzoMethodMHDVlct (EnzoMethodMHDVlct.cpp:90-152):
+ * validates the parameters (HLLC requires no_bfield, HLLE/HLLD require
+ * constrained_transport, theta in [1, 2], ...). */
+int mhdvlct_create(const MhdVlctParams* params, mhdvlct_handle** out);
+int mhdvlct_destroy(mhdvlct_handle* h);
+const char* mhdvlct_last_error_string(const mhdvlct_handle* h);
+/* Courant factor in effect (the "courant" key, default 0.3 for "vl" and 1 for
+ * "euler", EnzoMethodMHDVlct.cpp:100-101). */
+double mhdvlct_courant(const mhdvlct_handle* h);
+/* Sum of ghost depths the stages consume (NN + PLM = 3), the minimum ghost
+ * depth a block must have (EnzoMethodMHDVlct.cpp:124-133). */
+int mhdvlct_required_ghost_depth(const mhdvlct_handle* h);
+
+/* ------------------------------------------------------------ one block */
+typedef struct MhdBlockView {
+  int dtype;              /* MHD_DTYPE_F64 or MHD_DTYPE_F32                  */
+  int n[3];               /* active cells along x, y, z                      */
+  int ghost[3];           /* ghost depth along x, y, z (must be equal)       */
+  double cell_width[3];   /* EnzoBlock::CellWidth                            */
+  void* density;
+  void* velocity[3];      /* velocity_x/y/z (specific)                       */
+  void* total_energy;     /* specific total energy                           */
+  void* internal_energy;  /* specific internal energy (dual energy only)     */
+  void* bfield[3];        /* cell-centred bfield_x/y/z (MHD only)            */
+  void* bfieldi[3];       /* face-centred bfieldi_x/y/z (MHD only)           */
+  void* pressure;         /* [w] pressure field; may be NULL                 */
+} MhdBlockView;
+
+/* EnzoMethodMHDVlct::compute (EnzoMethodMHDVlct.cpp:356-500): one VL+CT step
+ * of size dt on a block whose ghost zones have been refreshed, in place. */
+int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b, double dt,
+                       void* stream);
+
+/* EnzoMethodMHDVlct::timestep (EnzoMethodMHDVlct.cpp:551-588): energy sync
+ * (dual energy), pressure field, courant * CFL dt over the whole ghosted
+ * block.  Synchronises `stream` to return dt on the host. */
+int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
+                           double* dt_out, void* stream);
+
+/* Same-level periodic ghost refresh of a block onto itself (the effect of
+ * Cello's refresh for a single periodic root block,
+ * src/Cello/control_refresh.cpp:243-360). */
+int mhdvlct_fill_ghosts_periodic(mhdvlct_handle* h, const MhdBlockView* b,
+                                 void* stream);
+
+/* ------------------------------------------------------------- batch
+ * Many blocks of possibly different sizes advanced together: one fused,
+ * persistent launch per stage over all blocks, the cycle captured as a CUDA
+ * graph.  Library-owned state; the caller reads/writes it through
+ * mhdvlct_batch_block_view (device pointers). */
+typedef struct mhdvlct_batch mhdvlct_batch;
+
+/* dims: nblocks x 3 active extents; widths: nblocks x 3 cell widths;
+ * ghost: ghost depth of every block; dtype: MHD_DTYPE_*. */
+int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
+                         const double* widths, int nblocks, int ghost,
+                         int dtype, mhdvlct_batch** out);
+int mhdvlct_batch_destroy(mhdvlct_batch* b);
+/* Device pointers of block i's current state (valid until the next step). */
+int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* out);
+/* nbr: nblocks x 27 block indices, nbr[27*i + (sz+1)*9 + (sy+1)*3 + (sx+1)]
+ * supplies the ghost region at offset (sx, sy, sz) of block i (same-size
+ * neighbours).  Default: every block is periodic on itself. */
+int mhdvlct_batch_set_neighbors(mhdvlct_batch* b, const int* nbr);
+/* Ghost refresh of every block from its neighbours. */
+int mhdvlct_batch_refresh(mhdvlct_batch* b, void* stream);
+/* One VL+CT step of every block; dt_per_block: host array of nblocks. */
+int mhdvlct_batch_step(mhdvlct_batch* b, const double* dt_per_block,
+                       void* stream);
+/* Per-block courant-limited dt (reference semantics, whole ghosted block);
+ * dt_out: host array of nblocks.  Synchronises the stream. */
+int mhdvlct_batch_timestep(mhdvlct_batch* b, double* dt_out, void* stream);
+/* Advance ncycles full cycles (timestep, refresh, two stages) entirely on
+ * the device: dt_mode 0 = one global dt (Cello's min-reduction), 1 = each
+ * block its own dt.  The cycle is captured once as a CUDA graph and
+ * replayed.  elapsed_time_out (may be NULL) receives the sum of dt. */
+int mhdvlct_batch_run(mhdvlct_batch* b, int ncycles, int dt_mode,
+                      double* elapsed_time_out, void* stream);
+/* Work decomposition: tile extent used per block size class (0 = auto). */
+int mhdvlct_batch_set_tile(mhdvlct_batch* b, int tile_x, int tile_y);
+
+/* ------------------------------------------------------------- serving
+ * Continuous batching of independent solves (each a periodic box of n^3
+ * cells), admitted against a device-memory budget. */
+typedef struct mhdserve mhdserve;
+typedef struct MhdServeRequest {
+  int n;                      /* active cells per side                      */
+  int cycles;                 /* number of VL+CT cycles                     */
+  char riemann_solver[16];
+  char reconstruct_method[16];
+  int mhd;                    /* 1: constrained_transport, 0: no_bfield     */
+  double box_size;            /* physical side length                       */
+  /* Initial state, host arrays of the block layout (caller keeps them until
+   * mhdserve_submit returns): density, vx, vy, vz, etot [, bx, by, bz,
+   * bfx, bfy, bfz]; float32. */
+  const float* init[12];
+} MhdServeRequest;
+
+int mhdserve_create(const MhdVlctParams* base, size_t hbm_budget_bytes,
+                    int max_active, mhdserve** out);
+int mhdserve_destroy(mhdserve* s);
+/* Queue a request; returns its ticket.  Rejected (MHD_ERR_NOMEM) if it could
+ * never fit in the budget, MHD_ERR_INVALID if malformed. */
+int mhdserve_submit(mhdserve* s, const MhdServeRequest* r, int* ticket);
+/* Run the scheduler for up to max_iterations iterations (one cycle of every
+ * active request per iteration); admits queued requests as memory frees. */
+int mhdserve_pump(mhdserve* s, int max_iterations);
+/* 0 = queued, 1 = running, 2 = done, 3 = failed */
+int mhdserve_poll(mhdserve* s, int ticket, int* state);
+/* Copy the final state (density, vx, vy, vz, etot[, bx, by, bz]) of a done
+ * request into host arrays of n^3 active cells each. */
+int mhdserve_result(mhdserve* s, int ticket, float* const* out_fields,
+                    double* sim_time_out);
+const char* mhdserve_last_error_string(const mhdserve* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MHDVLCT_GB300_H */

@@ -1,0 +1,244 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front-end of the CPU oracle.
+
+The oracle (vlct_oracle.cpp) restates Enzo-E's VL+CT step on the CPU.  Only
+tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use this
+module, and only as the checker or the timed CPU baseline; the product never
+imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle_vlct.so")
+
+HLLE, HLLC, HLLD = 0, 1, 2
+NN, PLM, PLM_ATHENA = 0, 1, 2
+
+CELL_FIELDS = ("rho", "vx", "vy", "vz", "etot", "eint", "bx", "by", "bz",
+               "pressure")
+FACE_FIELDS = ("bfx", "bfy", "bfz")
+
+
+class OracleParams(ctypes.Structure):
+    _fields_ = [("riemann", ctypes.c_int), ("recon", ctypes.c_int),
+                ("mhd", ctypes.c_int), ("dual_energy", ctypes.c_int),
+                ("euler", ctypes.c_int), ("eta", ctypes.c_double),
+                ("theta_limiter", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("density_floor", ctypes.c_double),
+                ("pressure_floor", ctypes.c_double),
+                ("courant", ctypes.c_double)]
+
+
+_P = ctypes.POINTER(ctypes.c_double)
+
+
+class OracleBlock(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("g", ctypes.c_int), ("dx", ctypes.c_double),
+                ("dy", ctypes.c_double), ("dz", ctypes.c_double)] + [
+                    (n, _P) for n in ("rho", "vx", "vy", "vz", "etot", "eint",
+                                      "bx", "by", "bz", "bfx", "bfy", "bfz",
+                                      "pressure")]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with the flags that keep the reference's FP order."""
+    src = os.path.join(HERE, "vlct_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or (
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(src)):
+        subprocess.check_call([
+            "g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+            "-fno-fast-math", "-o", LIB_PATH, src])
+    return LIB_PATH
+
+
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libvlct_ref.so")
+
+_lib = None
+_ref = None
+
+
+def ref_lib():
+    """The reference's own VL+CT sources built by oracle/Makefile (only where
+    the Enzo-E tree exists); None when it has not been built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB_PATH):
+        L = ctypes.CDLL(REF_LIB_PATH)
+        L.ref_step.argtypes = [ctypes.POINTER(OracleParams),
+                               ctypes.POINTER(OracleBlock), ctypes.c_double]
+        L.ref_step.restype = ctypes.c_int
+        L.ref_timestep.argtypes = [ctypes.POINTER(OracleParams),
+                                   ctypes.POINTER(OracleBlock)]
+        L.ref_timestep.restype = ctypes.c_double
+        _ref = L
+    return _ref
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oracle_step.argtypes = [ctypes.POINTER(OracleParams),
+                                  ctypes.POINTER(OracleBlock), ctypes.c_double]
+        L.oracle_step.restype = ctypes.c_int
+        L.oracle_timestep.argtypes = [ctypes.POINTER(OracleParams),
+                                      ctypes.POINTER(OracleBlock)]
+        L.oracle_timestep.restype = ctypes.c_double
+        L.oracle_fill_ghosts_periodic.argtypes = [ctypes.POINTER(OracleBlock)]
+        L.oracle_fill_ghosts_brick.argtypes = [ctypes.POINTER(OracleBlock),
+                                               ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int]
+        L.oracle_ic_inclined_wave.argtypes = [
+            ctypes.POINTER(OracleBlock), ctypes.c_char_p, ctypes.c_double,
+            ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+            ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.oracle_evolve_periodic.argtypes = [ctypes.POINTER(OracleParams),
+                                             ctypes.POINTER(OracleBlock),
+                                             ctypes.c_double, ctypes.c_int]
+        L.oracle_evolve_periodic.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def params(riemann=HLLD, recon=PLM, mhd=True, dual_energy=False, euler=False,
+           eta=0.001, theta_limiter=1.5, gamma=5.0 / 3.0, density_floor=1e-200,
+           pressure_floor=1e-200, courant=0.3) -> OracleParams:
+    return OracleParams(riemann, recon, int(mhd), int(dual_energy), int(euler),
+                        eta, theta_limiter, gamma, density_floor,
+                        pressure_floor, courant)
+
+
+class Block:
+    """One ghosted block held as float64 numpy arrays in Cello's layout."""
+
+    def __init__(self, n, g=3, widths=(1.0, 1.0, 1.0), mhd=True,
+                 dual_energy=False):
+        nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+        self.n = (nx, ny, nz)
+        self.g = g
+        self.widths = tuple(float(w) for w in widths)
+        mx, my, mz = nx + 2 * g, ny + 2 * g, nz + 2 * g
+        self.m = (mx, my, mz)
+        self.mhd = mhd
+        self.dual_energy = dual_energy
+        shp = (mz, my, mx)
+        self.f = {}
+        for k in ("rho", "vx", "vy", "vz", "etot", "pressure"):
+            self.f[k] = np.zeros(shp)
+        if dual_energy:
+            self.f["eint"] = np.zeros(shp)
+        if mhd:
+            for k in ("bx", "by", "bz"):
+                self.f[k] = np.zeros(shp)
+            self.f["bfx"] = np.zeros((mz, my, mx + 1))
+            self.f["bfy"] = np.zeros((mz, my + 1, mx))
+            self.f["bfz"] = np.zeros((mz + 1, my, mx))
+
+    def copy(self):
+        b = Block.__new__(Block)
+        b.__dict__.update(self.__dict__)
+        b.f = {k: v.copy() for k, v in self.f.items()}
+        return b
+
+    def cstruct(self) -> OracleBlock:
+        def p(k):
+            a = self.f.get(k)
+            if a is None:
+                return _P()
+            assert a.flags.c_contiguous and a.dtype == np.float64
+            return a.ctypes.data_as(_P)
+        nx, ny, nz = self.n
+        dx, dy, dz = self.widths
+        return OracleBlock(nx, ny, nz, self.g, dx, dy, dz,
+                           *[p(k) for k in ("rho", "vx", "vy", "vz", "etot",
+                                            "eint", "bx", "by", "bz", "bfx",
+                                            "bfy", "bfz", "pressure")])
+
+
+def step(prm: OracleParams, b: Block, dt: float, ref: bool = False) -> None:
+    cs = b.cstruct()
+    fn = ref_lib().ref_step if ref else lib().oracle_step
+    rc = fn(ctypes.byref(prm), ctypes.byref(cs), dt)
+    if rc != 0:
+        raise RuntimeError(f"oracle_step failed: {rc}")
+
+
+def timestep(prm: OracleParams, b: Block, ref: bool = False) -> float:
+    cs = b.cstruct()
+    fn = ref_lib().ref_timestep if ref else lib().oracle_timestep
+    return fn(ctypes.byref(prm), ctypes.byref(cs))
+
+
+def fill_ghosts_periodic(b: Block) -> None:
+    cs = b.cstruct()
+    lib().oracle_fill_ghosts_periodic(ctypes.byref(cs))
+
+
+def fill_ghosts_brick(blocks, nbx, nby, nbz) -> None:
+    arr = (OracleBlock * len(blocks))(*[b.cstruct() for b in blocks])
+    lib().oracle_fill_ghosts_brick(arr, nbx, nby, nbz)
+
+
+def inclined_wave(b: Block, wave: str, alpha=0.7297276562269663,
+                  beta=1.1071487177940904, gamma=1.6666666666666667,
+                  amplitude=1e-6, lam=1.0, positive_vel=True,
+                  lower=(0.0, 0.0, 0.0)) -> None:
+    cs = b.cstruct()
+    rc = lib().oracle_ic_inclined_wave(ctypes.byref(cs), wave.encode(), alpha,
+                                       beta, gamma, amplitude, lam,
+                                       int(positive_vel), *lower)
+    if rc != 0:
+        raise ValueError(f"unknown wave {wave}")
+
+
+def evolve_periodic(prm: OracleParams, b: Block, stop_time: float,
+                    max_cycles: int = 1 << 30, ref: bool = False) -> int:
+    """Cello's cycle on one periodic block: timestep on the current ghosts,
+    clip to the stop time, refresh the ghosts, step."""
+    if not ref:
+        cs = b.cstruct()
+        return lib().oracle_evolve_periodic(ctypes.byref(prm), ctypes.byref(cs),
+                                            stop_time, max_cycles)
+    time, cycle = 0.0, 0
+    while cycle < max_cycles:
+        dt = timestep(prm, b, ref=True)
+        dt = min(dt, stop_time - time)
+        if not time < stop_time:
+            break
+        fill_ghosts_periodic(b)
+        step(prm, b, dt, ref=True)
+        time += dt
+        cycle += 1
+    return cycle
+
+
+def pressure_of(b: Block, gamma: float) -> np.ndarray:
+    """Derived pressure over the whole block (EnzoComputePressure, no DE)."""
+    f = b.f
+    ke = 0.5 * (f["vx"] * f["vx"] + f["vy"] * f["vy"] + f["vz"] * f["vz"])
+    me = 0.0
+    if b.mhd:
+        me = 0.5 * (f["bx"] * f["bx"] + f["by"] * f["by"] + f["bz"] * f["bz"])
+    return (gamma - 1.0) * (f["rho"] * (f["etot"] - ke) - me)
+
+
+def l1_error_norm(a: Block, b: Block, fields, gamma: float, res: int) -> float:
+    """tools/l1_error_norm.py: sqrt(sum_f (sum |a-b| / res^3)^2) over the
+    active zone, with pressure derived from the state."""
+    g = a.g
+    nx, ny, nz = a.n
+    sl = (slice(g, g + nz), slice(g, g + ny), slice(g, g + nx))
+    errs = []
+    for k in fields:
+        if k == "pressure":
+            x, y = pressure_of(a, gamma), pressure_of(b, gamma)
+        else:
+            x, y = a.f[k], b.f[k]
+        errs.append(np.sum(np.abs(x[sl] - y[sl])) / float(res ** 3))
+    return float(np.sqrt(np.sum(np.square(errs))))

@@ -1,0 +1,147 @@
+"""Parity of the CUDA per-block path (through the C ABI) with the CPU oracle.
+
+FP64: fields within 1e-10 relative L1 after one step (the acceptance bar; in
+practice the FP64 path is bit-identical), dt and the ghost refresh bit-exact,
+div B at round-off.  FP32: per-field relative L1 against the FP64 oracle
+within 1e-5 per cycle.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from mhdvlct import block as B, ic
+from helpers import oracle_block, oracle_params, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # solver, recon, dual energy, time scheme
+    ("hlld", "plm", False, "vl"),
+    ("hlld", "nn", False, "vl"),
+    ("hlld", "plm_athena", False, "vl"),
+    ("hlle", "plm", False, "vl"),
+    ("hllc", "plm", False, "vl"),
+    ("hlld", "plm", True, "vl"),
+    ("hllc", "plm", True, "vl"),
+    ("hlld", "nn", False, "euler"),
+]
+
+
+def _pair(solver, recon, de, scheme, n=(8, 6, 7), seed=11, dtype=torch.float64,
+          theta=1.5):
+    mhd = solver != "hllc"
+    state, w = ic.smooth_block(n, 3, seed=seed, mhd=mhd, dual_energy=de)
+    meth = B.EnzoMethodMHDVlct(
+        mhd_choice="constrained_transport" if mhd else "no_bfield",
+        riemann_solver=solver, reconstruct_method=recon, time_scheme=scheme,
+        dual_energy=de, theta_limiter=theta)
+    blk = B.Block(n, 3, w, mhd=mhd, dual_energy=de, dtype=dtype)
+    blk.load_numpy(state)
+    ob = oracle_block(state, n, 3, w, mhd=mhd, de=de)
+    prm = oracle_params(solver, recon, de=de, euler=(scheme == "euler"),
+                        theta=theta, courant=meth.courant)
+    return meth, blk, ob, prm
+
+
+def _cmp(blk, ob, tol, exact_keys=()):
+    got = blk.to_numpy()
+    worst = {}
+    for k, a in got.items():
+        ref = ob.f[ic.ORACLE_NAME[k]]
+        e = rel_l1(a.astype(np.float64), ref)
+        worst[k] = e
+        assert e <= tol, (k, e)
+    for k in exact_keys:
+        assert np.array_equal(got[k], ob.f[ic.ORACLE_NAME[k]]), k
+    return worst
+
+
+@pytest.mark.parametrize("solver,recon,de,scheme", CASES)
+def test_fp64_step_matches_oracle(solver, recon, de, scheme):
+    meth, blk, ob, prm = _pair(solver, recon, de, scheme)
+    dt_o = O.timestep(prm, ob)
+    dt_g = meth.timestep(blk)
+    assert dt_g == dt_o
+    _cmp(blk, ob, 0.0)  # timestep writes pressure (+ dual-energy sync)
+    O.fill_ghosts_periodic(ob)
+    meth.fill_ghosts_periodic(blk)
+    _cmp(blk, ob, 0.0)
+    O.step(prm, ob, dt_o)
+    meth.compute(blk, dt_g)
+    torch.cuda.synchronize()
+    _cmp(blk, ob, 1e-10)
+
+
+@pytest.mark.parametrize("solver,recon,de,scheme", CASES[:3])
+def test_fp64_three_cycles_bit_exact(solver, recon, de, scheme):
+    meth, blk, ob, prm = _pair(solver, recon, de, scheme, n=8, seed=5)
+    for _ in range(3):
+        dt_o = O.timestep(prm, ob)
+        dt_g = meth.timestep(blk)
+        assert dt_g == dt_o
+        O.fill_ghosts_periodic(ob)
+        meth.fill_ghosts_periodic(blk)
+        O.step(prm, ob, dt_o)
+        meth.compute(blk, dt_g)
+    torch.cuda.synchronize()
+    got = blk.to_numpy()
+    for k, a in got.items():
+        assert np.array_equal(a, ob.f[ic.ORACLE_NAME[k]]), k
+
+
+def _divb(f, n, g, w):
+    nx, ny, nz = n
+    fx, fy, fz = f["bfieldi_x"], f["bfieldi_y"], f["bfieldi_z"]
+    sz, sy, sx = slice(g, g + nz), slice(g, g + ny), slice(g, g + nx)
+    return np.abs((fx[sz, sy, g + 1:g + nx + 1] - fx[sz, sy, g:g + nx]) / w[0] +
+                  (fy[sz, g + 1:g + ny + 1, sx] - fy[sz, g:g + ny, sx]) / w[1] +
+                  (fz[g + 1:g + nz + 1, sy, sx] - fz[g:g + nz, sy, sx]) / w[2]).max()
+
+
+@pytest.mark.parametrize("solver,recon", [("hlld", "plm"), ("hlle", "plm"),
+                                          ("hllc", "plm"), ("hlld", "nn")])
+def test_fp32_within_1e5_of_fp64_oracle(solver, recon):
+    meth, blk, ob, prm = _pair(solver, recon, False, "vl", n=12, seed=21,
+                               dtype=torch.float32)
+    for _ in range(2):
+        dt_o = O.timestep(prm, ob)
+        dt_g = meth.timestep(blk)
+        assert abs(dt_g - dt_o) / dt_o < 1e-6
+        O.fill_ghosts_periodic(ob)
+        meth.fill_ghosts_periodic(blk)
+        O.step(prm, ob, dt_o)
+        meth.compute(blk, dt_o)
+        torch.cuda.synchronize()
+        got = blk.to_numpy()
+        g = 3
+        act = (slice(g, g + 12),) * 3
+        for k in ("density", "velocity_x", "velocity_y", "velocity_z",
+                  "total_energy"):
+            e = rel_l1(got[k][act].astype(np.float64), ob.f[ic.ORACLE_NAME[k]][act])
+            assert e <= 1e-5, (k, e)
+    if solver != "hllc":
+        f = {k: v.astype(np.float64) for k, v in blk.to_numpy().items()}
+        assert _divb(f, (12, 12, 12), 3, blk.cell_width) <= 1e-6
+
+
+def test_fp64_div_b_roundoff():
+    meth, blk, ob, prm = _pair("hlld", "plm", False, "vl", n=10, seed=4)
+    for _ in range(4):
+        dt = meth.timestep(blk)
+        meth.fill_ghosts_periodic(blk)
+        meth.compute(blk, dt)
+    torch.cuda.synchronize()
+    assert _divb(blk.to_numpy(), (10, 10, 10), 3, blk.cell_width) <= 1e-13
+
+
+def test_invalid_arguments_are_rejected():
+    with pytest.raises(Exception):
+        B.EnzoMethodMHDVlct(mhd_choice="constrained_transport",
+                            riemann_solver="hllc")
+    with pytest.raises(Exception):
+        B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hlld")
+    meth = B.EnzoMethodMHDVlct()
+    blk = B.Block(8, 2, (0.1, 0.1, 0.1))  # ghost depth 2 < 3
+    with pytest.raises(Exception):
+        meth.compute(blk, 0.01)
