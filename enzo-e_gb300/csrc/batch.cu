@@ -1,0 +1,681 @@
+// batch.cu -- many blocks advanced together (the batched form).
+//
+// All blocks live in one library-owned device pool in Cello's per-field
+// layout.  A cycle is: timestep (reference semantics: whole ghosted block,
+// before the refresh), the global or per-block dt, the same-level ghost
+// refresh, and the two VL stages, each ONE persistent launch over the tiles of
+// every block (tiles sorted largest-first and pulled from a device work
+// queue).  The face-centred B is double buffered: the last stage reads the
+// start-of-step faces and writes the other buffer, so no stage updates a
+// field in place that another CTA may still read.  The whole cycle is
+// captured once as a CUDA graph per face-buffer parity and replayed.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "capi_internal.h"
+#include "vlct_aux.cuh"
+
+using namespace vlct;
+using namespace mhdint;
+
+namespace {
+
+__global__ void add_scalar_kernel(double* acc, const double* v) { *acc += *v; }
+
+struct TileChoice {
+  int tile_x = 0;  // x tile extent (0 = default)
+  int tile_y = 0;  // y tile extent (0 = default)
+  int zchunk = 0;  // z-chunk length (0 = whole block)
+};
+
+}  // namespace
+
+struct mhdvlct_batch {
+  mhdvlct_handle* h = nullptr;
+  int dtype = MHD_DTYPE_F32;
+  int nblocks = 0;
+  int g = 3;
+  std::vector<int> dims;       // 3 per block (active)
+  std::vector<double> widths;  // 3 per block
+  void* pool = nullptr;
+  size_t pool_bytes = 0;
+  size_t state_elems = 0;  // leading part of the pool holding the state
+  // element offsets (in units of the real type) of every array of block i
+  struct Off {
+    size_t ext[NCELL], tmp[NCELL], fa[3], fb[3], tf[3], pres;
+    int m[3];
+  };
+  std::vector<Off> off;
+  int parity = 0;  // 0: current faces in fa, 1: in fb
+  // device descriptors: [parity][stage] StageBlocks, [parity] AuxBlocks
+  void* d_sblocks[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  void* d_aux[2] = {nullptr, nullptr};
+  StageTile* d_tiles[2] = {nullptr, nullptr};
+  int ntiles[2] = {0, 0};
+  int tile_tx[2] = {0, 0}, tile_ty[2] = {0, 0};
+  int* d_queue = nullptr;     // 2 counters
+  int* d_nbr = nullptr;
+  double* d_dt = nullptr;     // per block
+  double* d_dtmin = nullptr;
+  double* d_time = nullptr;
+  void* d_smax = nullptr;
+  int grid = 0;               // persistent grid size of the stage launches
+  std::map<std::vector<int>, TileChoice> tune;  // per block-size class
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  std::string err;
+
+  template <class R> R* ptr(size_t o) const { return (R*)pool + o; }
+};
+
+namespace {
+
+int bfail(mhdvlct_batch* b, int code, const std::string& m) {
+  b->err = m;
+  if (b->h) b->h->err = m;
+  return code;
+}
+
+void drop_graphs(mhdvlct_batch* b) {
+  for (int p = 0; p < 2; p++)
+    for (int d = 0; d < 2; d++)
+      if (b->graph[p][d]) {
+        cudaGraphExecDestroy(b->graph[p][d]);
+        b->graph[p][d] = nullptr;
+      }
+}
+
+TileChoice choice_for(const mhdvlct_batch* b, int i) {
+  std::vector<int> key(b->dims.begin() + 3 * i, b->dims.begin() + 3 * i + 3);
+  auto it = b->tune.find(key);
+  TileChoice c;
+  if (it != b->tune.end()) c = it->second;
+  if (c.tile_x <= 0 || c.tile_y <= 0) {
+    const int t = default_tile(b->dtype, b->h->solver, b->h->recon, b->h->de);
+    c.tile_x = c.tile_y = t;
+  }
+  return c;
+}
+
+// (Re)build the descriptor arrays and tile lists on the device.
+template <class R>
+int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
+  const StagePlan sp = stage_plan(b->h);
+  if (sp.nstages != 2)
+    return bfail(b, MHD_ERR_INVALID, "the batched form runs the two-stage vl scheme");
+  std::vector<StageBlock<R>> sb[2][2];
+  std::vector<AuxBlock<R>> aux[2];
+  std::vector<StageTile> tiles[2];
+  int tx[2] = {1, 1}, ty[2] = {1, 1};
+  std::vector<std::pair<double, StageTile>> order[2];
+  for (int i = 0; i < b->nblocks; i++) {
+    const auto& O = b->off[i];
+    FieldSet<R> ext, tmp;
+    for (int k = 0; k < NCELL; k++) {
+      ext.c[k] = (O.ext[k] == (size_t)-1) ? nullptr : b->ptr<R>(O.ext[k]);
+      tmp.c[k] = (O.tmp[k] == (size_t)-1) ? nullptr : b->ptr<R>(O.tmp[k]);
+    }
+    for (int d = 0; d < 3; d++) tmp.f[d] = b->h->mhd ? b->ptr<R>(O.tf[d]) : nullptr;
+    for (int p = 0; p < 2; p++) {
+      FieldSet<R> cur_faces = ext, next_faces = ext;
+      for (int d = 0; d < 3; d++) {
+        R* fa = b->h->mhd ? b->ptr<R>(O.fa[d]) : nullptr;
+        R* fb = b->h->mhd ? b->ptr<R>(O.fb[d]) : nullptr;
+        cur_faces.f[d] = p == 0 ? fa : fb;
+        next_faces.f[d] = p == 0 ? fb : fa;
+      }
+      for (int s = 0; s < 2; s++) {
+        StageBlock<R> B;
+        for (int a = 0; a < 3; a++) {
+          B.m[a] = O.m[a];
+          B.cw[a] = b->widths[3 * i + a];
+        }
+        B.dt = b->d_dt + i;
+        B.base = cur_faces;
+        if (s == 0) {
+          B.cur = cur_faces;
+          B.out = tmp;
+        } else {
+          B.cur = tmp;
+          B.out = next_faces;  // cells in place, faces into the other buffer
+        }
+        sb[p][s].push_back(B);
+      }
+      AuxBlock<R> A;
+      for (int a = 0; a < 3; a++) {
+        A.m[a] = O.m[a];
+        A.cw[a] = b->widths[3 * i + a];
+      }
+      A.f = cur_faces;
+      A.pressure = b->ptr<R>(O.pres);
+      aux[p].push_back(A);
+    }
+    const TileChoice c = choice_for(b, i);
+    for (int s = 0; s < 2; s++) {
+      std::vector<StageTile> t;
+      make_tiles(i, O.m, sp.S[s], s == 1, c.tile_x, c.tile_y, c.zchunk, t);
+      for (auto& x : t) {
+        tx[s] = std::max(tx[s], x.xb - x.xa);
+        ty[s] = std::max(ty[s], x.yb - x.ya);
+        const double cost = (double)(x.xb - x.xa + 2) * (x.yb - x.ya + 2) *
+                            (x.zb - x.za + 2);
+        order[s].push_back({cost, x});
+      }
+    }
+  }
+  for (int s = 0; s < 2; s++) {
+    std::stable_sort(order[s].begin(), order[s].end(),
+                     [](const std::pair<double, StageTile>& a,
+                        const std::pair<double, StageTile>& c) { return a.first > c.first; });
+    for (auto& o : order[s]) tiles[s].push_back(o.second);
+    b->ntiles[s] = (int)tiles[s].size();
+    b->tile_tx[s] = tx[s];
+    b->tile_ty[s] = ty[s];
+  }
+  auto upload = [&](void** dst, const void* src, size_t bytes) -> int {
+    if (*dst) cudaFree(*dst);
+    *dst = nullptr;
+    if (cudaMalloc(dst, std::max<size_t>(bytes, 16)) != cudaSuccess)
+      return bfail(b, MHD_ERR_NOMEM, "descriptor allocation");
+    if (cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return bfail(b, MHD_ERR_CUDA, "descriptor upload");
+    return MHD_OK;
+  };
+  int rc;
+  for (int p = 0; p < 2; p++) {
+    for (int s = 0; s < 2; s++)
+      if ((rc = upload(&b->d_sblocks[p][s], sb[p][s].data(),
+                       sb[p][s].size() * sizeof(StageBlock<R>))))
+        return rc;
+    if ((rc = upload(&b->d_aux[p], aux[p].data(), aux[p].size() * sizeof(AuxBlock<R>))))
+      return rc;
+  }
+  for (int s = 0; s < 2; s++)
+    if ((rc = upload((void**)&b->d_tiles[s], tiles[s].data(),
+                     tiles[s].size() * sizeof(StageTile))))
+      return rc;
+  cudaStreamSynchronize(st);
+  drop_graphs(b);
+  return MHD_OK;
+}
+
+int build_descriptors_any(mhdvlct_batch* b, cudaStream_t st) {
+  return b->dtype == MHD_DTYPE_F64 ? build_descriptors<double>(b, st)
+                                   : build_descriptors<float>(b, st);
+}
+
+template <class R>
+cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
+  const StagePlan sp = stage_plan(b->h);
+  StageInfo info;
+  info.s = sp.s[s];
+  info.S = sp.S[s];
+  info.final_stage = s == 1;
+  info.dt_factor = sp.dt_factor[s];
+  info.tx = b->tile_tx[s];
+  info.ty = b->tile_ty[s];
+  info.queue = b->d_queue + s;
+  return launch_stage<R>(b->h->solver, sp.recon[s], b->h->de != 0,
+                         (const StageBlock<R>*)b->d_sblocks[b->parity][s],
+                         b->d_tiles[s], b->ntiles[s], info, b->h->phys, b->grid, st);
+}
+
+template <class R>
+cudaError_t launch_stages(mhdvlct_batch* b, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  for (int s = 0; s < 2; s++)
+    if ((e = launch_one_stage<R>(b, s, st)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+template <class R>
+cudaError_t launch_timestep_b(mhdvlct_batch* b, int global_min, cudaStream_t st) {
+  // chunks per block so that the grid covers the GPU a few times over
+  size_t cells = 0;
+  for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
+  const size_t per = std::max<size_t>(1, cells / b->nblocks);
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 2048, 64));
+  return launch_timestep<R>(b->h->mhd != 0, b->h->de != 0,
+                            (const AuxBlock<R>*)b->d_aux[b->parity], b->nblocks, cpb,
+                            b->h->phys, b->d_smax, b->h->params.courant, global_min,
+                            b->d_dt, b->d_dtmin, st);
+}
+
+template <class R>
+cudaError_t launch_refresh_b(mhdvlct_batch* b, cudaStream_t st) {
+  size_t cells = 0;
+  for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
+  const size_t per = std::max<size_t>(1, cells / b->nblocks);
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 4096, 32));
+  return launch_refresh<R>((const AuxBlock<R>*)b->d_aux[b->parity], b->d_nbr,
+                           b->nblocks, b->g, cpb, st);
+}
+
+template <class R>
+cudaError_t record_cycle(mhdvlct_batch* b, int dt_mode, cudaStream_t st) {
+  cudaError_t e = launch_timestep_b<R>(b, dt_mode == 0, st);
+  if (e != cudaSuccess) return e;
+  add_scalar_kernel<<<1, 1, 0, st>>>(b->d_time, b->d_dtmin);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_refresh_b<R>(b, st)) != cudaSuccess) return e;
+  return launch_stages<R>(b, st);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- C ABI
+extern "C" int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
+                                    const double* widths, int nblocks, int ghost,
+                                    int dtype, mhdvlct_batch** out) {
+  if (!h || !dims || !widths || !out || nblocks <= 0) return MHD_ERR_INVALID;
+  *out = nullptr;
+  if (dtype != MHD_DTYPE_F64 && dtype != MHD_DTYPE_F32)
+    return fail(h, MHD_ERR_INVALID, "unknown dtype");
+  if (h->euler) return fail(h, MHD_ERR_INVALID, "the batched form runs the vl scheme");
+  if (ghost < mhdvlct_required_ghost_depth(h))
+    return fail(h, MHD_ERR_GHOST, "ghost depth must be at least 3");
+  mhdvlct_batch* b = new mhdvlct_batch();
+  b->h = h;
+  b->dtype = dtype;
+  b->nblocks = nblocks;
+  b->g = ghost;
+  b->dims.assign(dims, dims + 3 * nblocks);
+  b->widths.assign(widths, widths + 3 * nblocks);
+  const size_t esz = dtype == MHD_DTYPE_F64 ? 8 : 4;
+  size_t o = 0;
+  auto take = [&](size_t n) {
+    const size_t r = o;
+    o += (n + 63) & ~(size_t)63;  // 256-byte aligned for FP32, 512 for FP64
+    return r;
+  };
+  b->off.resize(nblocks);
+  // state region (cell fields and both face buffers of every block) first,
+  // so that a bulk host transfer is one copy; scratch after it
+  for (int pass = 0; pass < 2; pass++) {
+    for (int i = 0; i < nblocks; i++) {
+      auto& O = b->off[i];
+      for (int a = 0; a < 3; a++) {
+        if (dims[3 * i + a] < 1 || !(widths[3 * i + a] > 0)) {
+          delete b;
+          return fail(h, MHD_ERR_INVALID, "bad block extents or widths");
+        }
+        O.m[a] = dims[3 * i + a] + 2 * ghost;
+      }
+      const size_t M = (size_t)O.m[0] * O.m[1] * O.m[2];
+      const size_t F[3] = {(size_t)(O.m[0] + 1) * O.m[1] * O.m[2],
+                           (size_t)O.m[0] * (O.m[1] + 1) * O.m[2],
+                           (size_t)O.m[0] * O.m[1] * (O.m[2] + 1)};
+      for (int k = 0; k < NCELL; k++) {
+        const bool used = (k != F_EINT || h->de) && (k < F_BX || h->mhd);
+        if (pass == 0) O.ext[k] = used ? take(M) : (size_t)-1;
+        else O.tmp[k] = used ? take(M) : (size_t)-1;
+      }
+      for (int d = 0; d < 3; d++) {
+        if (pass == 0) {
+          O.fa[d] = h->mhd ? take(F[d]) : (size_t)-1;
+          O.fb[d] = h->mhd ? take(F[d]) : (size_t)-1;
+        } else {
+          O.tf[d] = h->mhd ? take(F[d]) : (size_t)-1;
+        }
+      }
+      if (pass == 1) O.pres = take(M);
+    }
+    if (pass == 0) b->state_elems = o;
+  }
+  b->pool_bytes = o * esz;
+  cudaError_t e = cudaMalloc(&b->pool, b->pool_bytes);
+  if (e != cudaSuccess) {
+    delete b;
+    return fail(h, MHD_ERR_NOMEM, std::string("batch pool: ") + cudaGetErrorString(e));
+  }
+  cudaMemset(b->pool, 0, b->pool_bytes);
+  bool ok = cudaMalloc((void**)&b->d_queue, 2 * sizeof(int)) == cudaSuccess &&
+            cudaMalloc((void**)&b->d_nbr, 27 * sizeof(int) * (size_t)nblocks) == cudaSuccess &&
+            cudaMalloc((void**)&b->d_dt, sizeof(double) * (size_t)nblocks) == cudaSuccess &&
+            cudaMalloc((void**)&b->d_dtmin, sizeof(double)) == cudaSuccess &&
+            cudaMalloc((void**)&b->d_time, sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&b->d_smax, 3 * sizeof(unsigned long long) * (size_t)nblocks) == cudaSuccess;
+  if (!ok) {
+    mhdvlct_batch_destroy(b);
+    return fail(h, MHD_ERR_NOMEM, "batch descriptors");
+  }
+  cudaMemset(b->d_time, 0, sizeof(double));
+  std::vector<int> nbr(27 * (size_t)nblocks);
+  for (int i = 0; i < nblocks; i++)
+    for (int k = 0; k < 27; k++) nbr[27 * (size_t)i + k] = i;
+  cudaMemcpy(b->d_nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  b->grid = std::max(1, nsm) * 2;
+  if (int rc = build_descriptors_any(b, 0)) {
+    mhdvlct_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return MHD_OK;
+}
+
+extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
+  if (!b) return MHD_ERR_INVALID;
+  cudaDeviceSynchronize();
+  drop_graphs(b);
+  for (int p = 0; p < 2; p++) {
+    for (int s = 0; s < 2; s++) cudaFree(b->d_sblocks[p][s]);
+    cudaFree(b->d_aux[p]);
+  }
+  for (int s = 0; s < 2; s++) cudaFree(b->d_tiles[s]);
+  cudaFree(b->d_queue);
+  cudaFree(b->d_nbr);
+  cudaFree(b->d_dt);
+  cudaFree(b->d_dtmin);
+  cudaFree(b->d_time);
+  cudaFree(b->d_smax);
+  cudaFree(b->pool);
+  delete b;
+  return MHD_OK;
+}
+
+extern "C" int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* v) {
+  if (!b || !v || i < 0 || i >= b->nblocks) return MHD_ERR_INVALID;
+  std::memset(v, 0, sizeof(*v));
+  const auto& O = b->off[i];
+  const size_t esz = b->dtype == MHD_DTYPE_F64 ? 8 : 4;
+  char* base = (char*)b->pool;
+  auto p = [&](size_t o) -> void* { return o == (size_t)-1 ? nullptr : base + o * esz; };
+  v->dtype = b->dtype;
+  for (int a = 0; a < 3; a++) {
+    v->n[a] = b->dims[3 * i + a];
+    v->ghost[a] = b->g;
+    v->cell_width[a] = b->widths[3 * i + a];
+  }
+  v->density = p(O.ext[F_RHO]);
+  v->velocity[0] = p(O.ext[F_VX]);
+  v->velocity[1] = p(O.ext[F_VY]);
+  v->velocity[2] = p(O.ext[F_VZ]);
+  v->total_energy = p(O.ext[F_ETOT]);
+  v->internal_energy = p(O.ext[F_EINT]);
+  for (int d = 0; d < 3; d++) {
+    v->bfield[d] = p(O.ext[F_BX + d]);
+    v->bfieldi[d] = p(b->parity == 0 ? O.fa[d] : O.fb[d]);
+  }
+  v->pressure = p(O.pres);
+  return MHD_OK;
+}
+
+extern "C" int mhdvlct_batch_set_neighbors(mhdvlct_batch* b, const int* nbr) {
+  if (!b || !nbr) return MHD_ERR_INVALID;
+  for (int i = 0; i < b->nblocks; i++)
+    for (int k = 0; k < 27; k++) {
+      const int j = nbr[27 * (size_t)i + k];
+      if (j < 0 || j >= b->nblocks) return bfail(b, MHD_ERR_INVALID, "neighbour index out of range");
+      for (int a = 0; a < 3; a++)
+        if (b->dims[3 * j + a] != b->dims[3 * i + a])
+          return bfail(b, MHD_ERR_INVALID, "neighbours must have equal extents");
+    }
+  cudaError_t e = cudaMemcpy(b->d_nbr, nbr, 27 * sizeof(int) * (size_t)b->nblocks,
+                             cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? MHD_OK : bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int mhdvlct_batch_refresh(mhdvlct_batch* b, void* stream) {
+  if (!b) return MHD_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = b->dtype == MHD_DTYPE_F64 ? launch_refresh_b<double>(b, st)
+                                            : launch_refresh_b<float>(b, st);
+  return e == cudaSuccess ? MHD_OK : bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int mhdvlct_batch_step(mhdvlct_batch* b, const double* dt_per_block,
+                                  void* stream) {
+  if (!b || !dt_per_block) return MHD_ERR_INVALID;
+  for (int i = 0; i < b->nblocks; i++)
+    if (!(dt_per_block[i] > 0) || !std::isfinite(dt_per_block[i]))
+      return bfail(b, MHD_ERR_INVALID, "dt must be positive and finite");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(b->d_dt, dt_per_block, sizeof(double) * b->nblocks,
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = b->dtype == MHD_DTYPE_F64 ? launch_stages<double>(b, st) : launch_stages<float>(b, st);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  b->parity ^= 1;
+  return MHD_OK;
+}
+
+extern "C" int mhdvlct_batch_timestep(mhdvlct_batch* b, double* dt_out, void* stream) {
+  if (!b || !dt_out) return MHD_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = b->dtype == MHD_DTYPE_F64 ? launch_timestep_b<double>(b, 0 + 0, st)
+                                            : launch_timestep_b<float>(b, 0, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dt_out, b->d_dt, sizeof(double) * b->nblocks,
+                        cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? MHD_OK : bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int mhdvlct_batch_run(mhdvlct_batch* b, int ncycles, int dt_mode,
+                                 double* elapsed_out, void* stream) {
+  if (!b || ncycles < 0 || (dt_mode != 0 && dt_mode != 1)) return MHD_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the simulated-time accumulator restarts with every call that advances;
+  // a call with ncycles == 0 just reads it
+  cudaError_t e = ncycles > 0 ? cudaMemsetAsync(b->d_time, 0, sizeof(double), st)
+                              : cudaSuccess;
+  for (int c = 0; c < ncycles && e == cudaSuccess; c++) {
+    cudaGraphExec_t& ge = b->graph[b->parity][dt_mode];
+    if (!ge) {
+      // capture this parity's cycle once on a private stream
+      cudaStream_t cs;
+      if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+      cudaGraph_t gph = nullptr;
+      e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = b->dtype == MHD_DTYPE_F64 ? record_cycle<double>(b, dt_mode, cs)
+                                                   : record_cycle<float>(b, dt_mode, cs);
+        e = cudaStreamEndCapture(cs, &gph);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, gph, 0);
+      if (gph) cudaGraphDestroy(gph);
+      cudaStreamDestroy(cs);
+      if (e != cudaSuccess) {
+        ge = nullptr;
+        break;
+      }
+    }
+    e = cudaGraphLaunch(ge, st);
+    b->parity ^= 1;
+  }
+  if (e == cudaSuccess && elapsed_out) {
+    e = cudaMemcpyAsync(elapsed_out, b->d_time, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  return e == cudaSuccess ? MHD_OK : bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int mhdvlct_batch_set_tile(mhdvlct_batch* b, int tile_x, int tile_y) {
+  if (!b || tile_x < 0 || tile_y < 0) return MHD_ERR_INVALID;
+  const int tmax = b->dtype == MHD_DTYPE_F64 ? TileLimits<double>::TMAX
+                                             : TileLimits<float>::TMAX;
+  if (tile_x > tmax || tile_y > tmax) return bfail(b, MHD_ERR_INVALID, "tile too large");
+  b->tune.clear();
+  for (int i = 0; i < b->nblocks; i++) {
+    std::vector<int> key(b->dims.begin() + 3 * i, b->dims.begin() + 3 * i + 3);
+    TileChoice c;
+    c.tile_x = tile_x;
+    c.tile_y = tile_y;
+    b->tune[key] = c;
+  }
+  return build_descriptors_any(b, 0);
+}
+
+extern "C" int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,
+                                          size_t* bytes) {
+  if (!b || !dev_ptr || !bytes) return MHD_ERR_INVALID;
+  *dev_ptr = b->pool;
+  *bytes = b->state_elems * (b->dtype == MHD_DTYPE_F64 ? 8 : 4);
+  return MHD_OK;
+}
+
+namespace {
+template <class R>
+int profile_t(mhdvlct_batch* b, int reps, int dt_mode, float* ms, cudaStream_t st) {
+  cudaEvent_t ev[5];
+  for (auto& e : ev) cudaEventCreate(&e);
+  double acc[5] = {0, 0, 0, 0, 0};
+  cudaError_t e = cudaSuccess;
+  for (int r = 0; r < reps && e == cudaSuccess; r++) {
+    cudaEventRecord(ev[0], st);
+    e = launch_timestep_b<R>(b, dt_mode == 0, st);
+    cudaEventRecord(ev[1], st);
+    if (e == cudaSuccess) e = launch_refresh_b<R>(b, st);
+    cudaEventRecord(ev[2], st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess) e = launch_one_stage<R>(b, 0, st);
+    cudaEventRecord(ev[3], st);
+    if (e == cudaSuccess) e = launch_one_stage<R>(b, 1, st);
+    cudaEventRecord(ev[4], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+    b->parity ^= 1;
+    float t;
+    for (int k = 0; k < 4; k++) {
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      acc[k] += t;
+    }
+    cudaEventElapsedTime(&t, ev[0], ev[4]);
+    acc[4] += t;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  for (int k = 0; k < 5; k++) ms[k] = (float)(acc[k] / std::max(1, reps));
+  return MHD_OK;
+}
+
+template <class R>
+int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
+  // save the state so the trial steps leave no trace
+  const size_t bytes = b->state_elems * sizeof(R);
+  void* save = nullptr;
+  if (cudaMalloc(&save, bytes) != cudaSuccess)
+    return bfail(b, MHD_ERR_NOMEM, "autotune state copy");
+  const int parity0 = b->parity;
+  cudaMemcpyAsync(save, b->pool, bytes, cudaMemcpyDeviceToDevice, st);
+  // a dt for the trial steps (per-block CFL of the current state)
+  cudaError_t e = launch_timestep_b<R>(b, 0, st);
+  if (e != cudaSuccess) {
+    cudaFree(save);
+    return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  }
+  const int tmax = TileLimits<R>::TMAX;
+  std::vector<std::vector<int>> classes;
+  for (int i = 0; i < b->nblocks; i++) {
+    std::vector<int> key(b->dims.begin() + 3 * i, b->dims.begin() + 3 * i + 3);
+    if (std::find(classes.begin(), classes.end(), key) == classes.end())
+      classes.push_back(key);
+  }
+  // largest classes first: they dominate the cost
+  std::sort(classes.begin(), classes.end(), [](const std::vector<int>& a,
+                                               const std::vector<int>& c) {
+    return (long)a[0] * a[1] * a[2] > (long)c[0] * c[1] * c[2];
+  });
+  const size_t smem_cap = 220 * 1024;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  json = "{";
+  bool first_cls = true;
+  for (const auto& cls : classes) {
+    const int m_lat = std::max(cls[0], cls[1]) + 2 * b->g;
+    std::vector<TileChoice> cands;
+    for (int ty = 4; ty <= tmax; ty += 2)
+      for (int tx = ty; tx <= std::min(tmax, 2 * ty); tx += ty) {
+        if (stage_smem<R>(b->h->solver, b->h->recon, b->h->de != 0, tx, ty) > smem_cap)
+          continue;
+        if (tx > m_lat || ty > m_lat) continue;
+        for (int zc : {0, 16, 32}) {
+          if (zc && zc >= cls[2]) continue;
+          TileChoice c;
+          c.tile_x = tx;
+          c.tile_y = ty;
+          c.zchunk = zc;
+          cands.push_back(c);
+        }
+      }
+    float best = 1e30f;
+    int rep_block = 0;
+    for (int i = 0; i < b->nblocks; i++)
+      if (b->dims[3 * i] == cls[0] && b->dims[3 * i + 1] == cls[1] &&
+          b->dims[3 * i + 2] == cls[2]) {
+        rep_block = i;
+        break;
+      }
+    TileChoice bestc = choice_for(b, rep_block);
+    for (const auto& c : cands) {
+      b->tune[cls] = c;
+      if (int rc = build_descriptors<R>(b, st)) {
+        cudaFree(save);
+        return rc;
+      }
+      // one untimed step, then reps timed steps
+      e = launch_stages<R>(b, st);
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch_stages<R>(b, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) break;
+      float t;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (t < best) {
+        best = t;
+        bestc = c;
+      }
+    }
+    b->tune[cls] = bestc;
+    char buf[256];
+    std::snprintf(buf, sizeof(buf),
+                  "%s\"%dx%dx%d\": {\"tile_x\": %d, \"tile_y\": %d, \"zchunk\": %d, "
+                  "\"ms_per_step\": %.4f, \"candidates\": %zu}",
+                  first_cls ? "" : ", ", cls[0], cls[1], cls[2], bestc.tile_x,
+                  bestc.tile_y, bestc.zchunk, best / std::max(1, reps), cands.size());
+    json += buf;
+    first_cls = false;
+    if (e != cudaSuccess) break;
+  }
+  json += "}";
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->parity = parity0;
+  cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
+  cudaStreamSynchronize(st);
+  cudaFree(save);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  return build_descriptors<R>(b, st);
+}
+}  // namespace
+
+extern "C" int mhdvlct_batch_profile(mhdvlct_batch* b, int reps, int dt_mode,
+                                     float* ms_out, void* stream) {
+  if (!b || !ms_out || reps < 1) return MHD_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? profile_t<double>(b, reps, dt_mode, ms_out, st)
+                                   : profile_t<float>(b, reps, dt_mode, ms_out, st);
+}
+
+extern "C" int mhdvlct_batch_autotune(mhdvlct_batch* b, int reps, char* json_out,
+                                      size_t json_len, void* stream) {
+  if (!b || reps < 1) return MHD_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::string json;
+  int rc = b->dtype == MHD_DTYPE_F64 ? autotune_t<double>(b, reps, json, st)
+                                     : autotune_t<float>(b, reps, json, st);
+  if (json_out && json_len) std::snprintf(json_out, json_len, "%s", json.c_str());
+  return rc;
+}

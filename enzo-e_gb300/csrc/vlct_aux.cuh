@@ -190,10 +190,16 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
   const AuxBlock<R>& B = blocks[b];
   const int n[3] = {B.m[0] - 2 * g, B.m[1] - 2 * g, B.m[2] - 2 * g};
   for (int fs = 0; fs < nfield_slots; fs++) {
-    // slots 0..8 cell fields, 9..11 face fields
-    R* dst = (fs < NCELL) ? B.f.c[fs] : B.f.f[fs - NCELL];
+    // slots 0..8 cell fields, 9..11 face fields, 12 the pressure field
+    // (Cello refreshes every field, EnzoMethodMHDVlct.cpp:146-151)
+    auto slot_ptr = [&](const AuxBlock<R>& X) -> R* {
+      if (fs < NCELL) return X.f.c[fs];
+      if (fs < NCELL + 3) return X.f.f[fs - NCELL];
+      return X.pressure;
+    };
+    R* dst = slot_ptr(B);
     if (!dst) continue;
-    const int face = (fs < NCELL) ? -1 : fs - NCELL;
+    const int face = (fs >= NCELL && fs < NCELL + 3) ? fs - NCELL : -1;
     int e[3], lo[3], hi[3];
     for (int a = 0; a < 3; a++) {
       e[a] = B.m[a] + (a == face);
@@ -245,7 +251,7 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
       }
       const int sb = nbr[27 * b + (side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1)];
       const AuxBlock<R>& SB = blocks[sb];
-      const R* sp = (fs < NCELL) ? SB.f.c[fs] : SB.f.f[fs - NCELL];
+      const R* sp = slot_ptr(SB);
       dst[((size_t)z * e[1] + y) * e[0] + x] = sp[((size_t)src[2] * e[1] + src[1]) * e[0] + src[0]];
     }
   }

@@ -109,7 +109,7 @@ cudaError_t launch_timestep<VLCT_REAL>(bool mhd, bool de,
 template <>
 cudaError_t launch_refresh<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, const int* nbr,
                                       int nb, int g, int cpb, cudaStream_t st) {
-  refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 3, cpb);
+  refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 4, cpb);
   return cudaGetLastError();
 }
 

@@ -136,7 +136,14 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   const R theta = R(phys.theta_limiter);
   const R dfloor = R(phys.density_floor), pfloor = R(phys.pressure_floor);
 
-  for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
+  __shared__ int s_next;
+  int it = blockIdx.x;
+  if (info.queue) {
+    if (tid == 0) s_next = atomicAdd(info.queue, 1);
+    __syncthreads();
+    it = s_next;
+  }
+  while (it < ntiles) {
     const StageTile tl = tiles[it];
     const StageBlock<R>& B = blocks[tl.block];
     const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
@@ -555,6 +562,15 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         }
       }
       __syncthreads();
+    }
+    // next tile: dynamic queue (persistent grid) or static grid stride
+    if (info.queue) {
+      if (tid == 0) s_next = atomicAdd(info.queue, 1);
+      __syncthreads();
+      it = s_next;
+      __syncthreads();
+    } else {
+      it += gridDim.x;
     }
   }
 }

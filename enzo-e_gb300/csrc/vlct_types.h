@@ -49,6 +49,8 @@ struct StageInfo {
   int final_stage;  // 1 on the last stage (writes layer S of centred B)
   double dt_factor; // 0.5 for the half step, 1 for the full step
   int tx, ty;       // maximum tile extent of the launch (sizes shared memory)
+  int* queue;       // work counter (zeroed before the launch) for a persistent
+                    // grid pulling tiles dynamically; null = static grid stride
 };
 
 }  // namespace vlct

@@ -32,9 +32,10 @@ EXPORTED = (
     "mhdvlct_batch_create", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
     "mhdvlct_batch_refresh", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
-    "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdserve_create",
+    "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_autotune",
+    "mhdvlct_batch_state_region", "mhdvlct_batch_profile", "mhdserve_create",
     "mhdserve_destroy", "mhdserve_submit", "mhdserve_pump", "mhdserve_poll",
-    "mhdserve_result", "mhdserve_last_error_string",
+    "mhdserve_result", "mhdserve_timing", "mhdserve_last_error_string",
 )
 
 
@@ -114,12 +115,16 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_batch_timestep.argtypes = [vp, P(dp), vp]
     L.mhdvlct_batch_run.argtypes = [vp, ip, ip, P(dp), vp]
     L.mhdvlct_batch_set_tile.argtypes = [vp, ip, ip]
+    L.mhdvlct_batch_autotune.argtypes = [vp, ip, ctypes.c_char_p, ctypes.c_size_t, vp]
+    L.mhdvlct_batch_state_region.argtypes = [vp, P(vp), P(ctypes.c_size_t)]
+    L.mhdvlct_batch_profile.argtypes = [vp, ip, ip, P(ctypes.c_float), vp]
     L.mhdserve_create.argtypes = [P(MhdVlctParams), ctypes.c_size_t, ip, P(vp)]
     L.mhdserve_destroy.argtypes = [vp]
     L.mhdserve_submit.argtypes = [vp, P(MhdServeRequest), P(ip)]
     L.mhdserve_pump.argtypes = [vp, ip]
     L.mhdserve_poll.argtypes = [vp, ip, P(ip)]
     L.mhdserve_result.argtypes = [vp, ip, P(ctypes.c_void_p), P(dp)]
+    L.mhdserve_timing.argtypes = [vp, ip, P(dp), P(dp), P(dp)]
     L.mhdserve_last_error_string.argtypes = [vp]
     L.mhdserve_last_error_string.restype = ctypes.c_char_p
     _lib = L

@@ -163,6 +163,21 @@ int mhdvlct_batch_run(mhdvlct_batch* b, int ncycles, int dt_mode,
                       double* elapsed_time_out, void* stream);
 /* Work decomposition: tile extent used per block size class (0 = auto). */
 int mhdvlct_batch_set_tile(mhdvlct_batch* b, int tile_x, int tile_y);
+/* The autotuner: for every block-size class, time candidate (tile, z-chunk)
+ * work decompositions on the batch's own data and keep the fastest.  The
+ * state is restored afterwards.  json_out (may be NULL) receives a JSON
+ * description of the choices. */
+int mhdvlct_batch_autotune(mhdvlct_batch* b, int reps, char* json_out,
+                           size_t json_len, void* stream);
+/* Device address and size of the contiguous region holding every block's
+ * state (cell fields and both face-B buffers), for bulk host transfers. */
+int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,
+                               size_t* bytes);
+/* Run `reps` cycles as individual launches with CUDA events between the
+ * kernels; ms_out[0..4] = mean ms per cycle of the timestep reduction, the
+ * ghost refresh, stage 1 (half dt), stage 2 (full dt) and the whole cycle. */
+int mhdvlct_batch_profile(mhdvlct_batch* b, int reps, int dt_mode,
+                          float* ms_out, void* stream);
 
 /* ------------------------------------------------------------- serving
  * Continuous batching of independent solves (each a periodic box of n^3
@@ -175,9 +190,10 @@ typedef struct MhdServeRequest {
   char reconstruct_method[16];
   int mhd;                    /* 1: constrained_transport, 0: no_bfield     */
   double box_size;            /* physical side length                       */
-  /* Initial state, host arrays of the block layout (caller keeps them until
-   * mhdserve_submit returns): density, vx, vy, vz, etot [, bx, by, bz,
-   * bfx, bfy, bfz]; float32. */
+  /* Initial state as float32 host arrays in the ghosted block layout of an
+   * n^3 block with 3 ghost layers (copied by mhdserve_submit): density,
+   * velocity_x/y/z, total_energy and, with mhd, bfield_x/y/z and
+   * bfieldi_x/y/z.  The ghost zones are refreshed periodically on admission. */
   const float* init[12];
 } MhdServeRequest;
 
@@ -196,6 +212,10 @@ int mhdserve_poll(mhdserve* s, int ticket, int* state);
  * request into host arrays of n^3 active cells each. */
 int mhdserve_result(mhdserve* s, int ticket, float* const* out_fields,
                     double* sim_time_out);
+/* Host wall-clock seconds (steady clock) of a request's submission,
+ * admission and completion. */
+int mhdserve_timing(mhdserve* s, int ticket, double* t_submit, double* t_admit,
+                    double* t_done);
 const char* mhdserve_last_error_string(const mhdserve* s);
 
 #ifdef __cplusplus

@@ -1,0 +1,196 @@
+"""The batched form: many blocks in one persistent launch per stage.
+
+Checks (FP64, bit-exact against the per-block oracle): one batched step on a
+set of uneven blocks; the neighbour-table ghost refresh of a periodic brick
+against the oracle's multi-block refresh; a graph-captured multi-cycle run
+against the oracle's cycle (timestep on stale ghosts, global min dt,
+refresh, step)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from mhdvlct import block as B, capi, ic
+from helpers import oracle_block, oracle_params
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
+        "bfield_x", "bfield_y", "bfield_z", "bfieldi_x", "bfieldi_y",
+        "bfieldi_z")
+
+
+class Batch:
+    def __init__(self, meth, dims, widths, dtype=capi.MHD_DTYPE_F64):
+        n = len(dims)
+        d = (ctypes.c_int * (3 * n))(*[int(v) for t in dims for v in t])
+        w = (ctypes.c_double * (3 * n))(*[float(v) for t in widths for v in t])
+        h = ctypes.c_void_p()
+        rc = capi.lib().mhdvlct_batch_create(meth.handle, d, w, n, 3, dtype,
+                                             ctypes.byref(h))
+        capi.check(rc, meth.handle, "batch_create")
+        self.h, self.meth, self.n = h, meth, n
+        self.dims, self.dtype = dims, dtype
+
+    def view(self, i):
+        v = capi.MhdBlockView()
+        capi.check(capi.lib().mhdvlct_batch_block_view(self.h, i, ctypes.byref(v)))
+        return v
+
+    def tensors(self, i):
+        """torch views (sharing memory) of block i's current fields"""
+        v = self.view(i)
+        nx, ny, nz = v.n[0], v.n[1], v.n[2]
+        g = v.ghost[0]
+        mx, my, mz = nx + 2 * g, ny + 2 * g, nz + 2 * g
+        out = {}
+        ptrs = {"density": v.density, "velocity_x": v.velocity[0],
+                "velocity_y": v.velocity[1], "velocity_z": v.velocity[2],
+                "total_energy": v.total_energy, "bfield_x": v.bfield[0],
+                "bfield_y": v.bfield[1], "bfield_z": v.bfield[2],
+                "bfieldi_x": v.bfieldi[0], "bfieldi_y": v.bfieldi[1],
+                "bfieldi_z": v.bfieldi[2], "pressure": v.pressure}
+        shapes = {"bfieldi_x": (mz, my, mx + 1), "bfieldi_y": (mz, my + 1, mx),
+                  "bfieldi_z": (mz + 1, my, mx)}
+        for k, p in ptrs.items():
+            if p:
+                out[k] = (p, shapes.get(k, (mz, my, mx)))
+        return out
+
+    def upload(self, i, state):
+        dt = np.float64 if self.dtype == capi.MHD_DTYPE_F64 else np.float32
+        for k, (p, shp) in self.tensors(i).items():
+            if k in state:
+                a = np.ascontiguousarray(state[k], dtype=dt)
+                assert a.shape == shp, (k, a.shape, shp)
+                torch.cuda.synchronize()
+                ctypes_cuda_memcpy(p, a, to_device=True)
+
+    def download(self, i):
+        dt = np.float64 if self.dtype == capi.MHD_DTYPE_F64 else np.float32
+        out = {}
+        torch.cuda.synchronize()
+        for k, (p, shp) in self.tensors(i).items():
+            a = np.empty(shp, dtype=dt)
+            ctypes_cuda_memcpy(p, a, to_device=False)
+            out[k] = a
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            capi.lib().mhdvlct_batch_destroy(self.h)
+            self.h = None
+
+
+_cudart = None
+
+
+def ctypes_cuda_memcpy(dev_ptr, host_arr, to_device):
+    """cudaMemcpy through the CUDA runtime the library itself loaded."""
+    global _cudart
+    if _cudart is None:
+        capi.lib()
+        path = None
+        with open("/proc/self/maps") as f:
+            for line in f:
+                if "libcudart" in line:
+                    path = line.split()[-1]
+                    break
+        _cudart = ctypes.CDLL(path or "libcudart.so")
+        _cudart.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_size_t, ctypes.c_int]
+    n = host_arr.nbytes
+    if to_device:
+        rc = _cudart.cudaMemcpy(dev_ptr, host_arr.ctypes.data, n, 1)
+    else:
+        rc = _cudart.cudaMemcpy(host_arr.ctypes.data, dev_ptr, n, 2)
+    assert rc == 0, rc
+
+
+def test_batched_step_uneven_blocks_bit_exact():
+    meth = B.EnzoMethodMHDVlct()
+    sizes = [(8, 8, 8), (6, 10, 7), (12, 8, 8), (8, 8, 8)]
+    states, widths = [], []
+    for i, n in enumerate(sizes):
+        s, w = ic.smooth_block(n, 3, seed=100 + i)
+        states.append(s)
+        widths.append(w)
+    bt = Batch(meth, sizes, widths)
+    for i, s in enumerate(states):
+        bt.upload(i, s)
+    capi.check(capi.lib().mhdvlct_batch_refresh(bt.h, None))
+    dts = (ctypes.c_double * len(sizes))(*[0.004, 0.003, 0.002, 0.005])
+    capi.check(capi.lib().mhdvlct_batch_step(bt.h, dts, None))
+    prm = oracle_params(courant=meth.courant)
+    for i, (s, n, w) in enumerate(zip(states, sizes, widths)):
+        ob = oracle_block(s, n, 3, w)
+        O.fill_ghosts_periodic(ob)
+        O.step(prm, ob, dts[i])
+        got = bt.download(i)
+        for k in KEYS:
+            g = 3
+            ref = ob.f[ic.ORACLE_NAME[k]]
+            if k.startswith("bfieldi"):
+                # the batch's current face buffer holds the updated interior
+                d = "xyz".index(k[-1])
+                sl = [slice(g, g + nn) for nn in reversed(n)]
+                sl[2 - d] = slice(g, g + n[d] + 1)
+                a, r = got[k][tuple(sl)], ref[tuple(sl)]
+            else:
+                a, r = got[k], ref
+            assert np.array_equal(a, r), (i, k, np.abs(a - r).max())
+
+
+def test_brick_refresh_matches_oracle():
+    meth = B.EnzoMethodMHDVlct()
+    blocks, w = ic.turbulent_box(N=16, nb=2, g=3, seed=3)
+    for blk in blocks:  # scramble ghosts so the refresh has work to do
+        for k, a in blk.items():
+            a[:3] = -1.0
+    nb = 2
+    bt = Batch(meth, [(8, 8, 8)] * 8, [w] * 8)
+    nbr = ic.brick_neighbors(nb)
+    arr = (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())
+    capi.check(capi.lib().mhdvlct_batch_set_neighbors(bt.h, arr))
+    for i, s in enumerate(blocks):
+        bt.upload(i, s)
+    capi.check(capi.lib().mhdvlct_batch_refresh(bt.h, None))
+    obs = [oracle_block(s, 8, 3, w) for s in blocks]
+    O.fill_ghosts_brick(obs, nb, nb, nb)
+    for i in range(8):
+        got = bt.download(i)
+        for k in KEYS:
+            assert np.array_equal(got[k], obs[i].f[ic.ORACLE_NAME[k]]), (i, k)
+
+
+def test_graph_run_matches_oracle_cycles():
+    meth = B.EnzoMethodMHDVlct()
+    nb, N = 2, 16
+    blocks, w = ic.turbulent_box(N=N, nb=nb, g=3, seed=9, mach=1.0)
+    bt = Batch(meth, [(8, 8, 8)] * 8, [w] * 8)
+    nbr = ic.brick_neighbors(nb)
+    capi.check(capi.lib().mhdvlct_batch_set_neighbors(
+        bt.h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())))
+    for i, s in enumerate(blocks):
+        bt.upload(i, s)
+    ncyc = 3
+    t = ctypes.c_double()
+    capi.check(capi.lib().mhdvlct_batch_run(bt.h, ncyc, 0, ctypes.byref(t), None))
+    prm = oracle_params(courant=meth.courant)
+    obs = [oracle_block(s, 8, 3, w) for s in blocks]
+    tt = 0.0
+    for _ in range(ncyc):
+        dt = min(O.timestep(prm, ob) for ob in obs)
+        O.fill_ghosts_brick(obs, nb, nb, nb)
+        for ob in obs:
+            O.step(prm, ob, dt)
+        tt += dt
+    assert t.value == tt
+    for i in range(8):
+        got = bt.download(i)
+        g = 3
+        act = (slice(g, g + 8),) * 3
+        for k in KEYS[:8]:
+            assert np.array_equal(got[k][act], obs[i].f[ic.ORACLE_NAME[k]][act]), (i, k)
