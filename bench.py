@@ -57,6 +57,8 @@ def _args():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--cpu-sample-blocks", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tile", type=str, default="",
+                    help="force the stage tile, e.g. 24x12 (skips the autotuner)")
     return ap.parse_args()
 
 
@@ -307,7 +309,11 @@ def main():
     # ---------------------------------------------------- batched FP32 form
     h32 = make_batch(meth, blocks, widths, capi.MHD_DTYPE_F32, a.nb)
     tune = None
-    if not a.no_tune:
+    if a.tile:
+        tx, ty = (int(v) for v in a.tile.lower().split("x"))
+        capi.check(L.mhdvlct_batch_set_tile(h32, tx, ty), meth.handle, "tile")
+        tune = {"forced_tile": a.tile}
+    elif not a.no_tune:
         buf = ctypes.create_string_buffer(4096)
         capi.check(L.mhdvlct_batch_autotune(h32, 2, buf, 4096, sp), meth.handle,
                    "autotune")

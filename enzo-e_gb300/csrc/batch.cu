@@ -20,6 +20,7 @@
 
 #include "capi_internal.h"
 #include "vlct_aux.cuh"
+#include "vlct_stage.cuh"
 
 using namespace vlct;
 using namespace mhdint;
@@ -65,7 +66,8 @@ struct mhdvlct_batch {
   double* d_dtmin = nullptr;
   double* d_time = nullptr;
   void* d_smax = nullptr;
-  int grid = 0;               // persistent grid size of the stage launches
+  int grid = 0;               // persistent grid size (0 = fill the GPU)
+  int threads = 256;          // CTA size of the stage launches
   std::map<std::vector<int>, TileChoice> tune;  // per block-size class
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   std::string err;
@@ -220,6 +222,7 @@ cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
   info.tx = b->tile_tx[s];
   info.ty = b->tile_ty[s];
   info.queue = b->d_queue + s;
+  info.threads = b->threads;
   return launch_stage<R>(b->h->solver, sp.recon[s], b->h->de != 0,
                          (const StageBlock<R>*)b->d_sblocks[b->parity][s],
                          b->d_tiles[s], b->ntiles[s], info, b->h->phys, b->grid, st);
@@ -350,10 +353,7 @@ extern "C" int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
   for (int i = 0; i < nblocks; i++)
     for (int k = 0; k < 27; k++) nbr[27 * (size_t)i + k] = i;
   cudaMemcpy(b->d_nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice);
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  b->grid = std::max(1, nsm) * 2;
+  b->grid = 0;
   if (int rc = build_descriptors_any(b, 0)) {
     mhdvlct_batch_destroy(b);
     return rc;
@@ -585,7 +585,7 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
                                                const std::vector<int>& c) {
     return (long)a[0] * a[1] * a[2] > (long)c[0] * c[1] * c[2];
   });
-  const size_t smem_cap = 220 * 1024;
+  const size_t smem_cap = 227 * 1024;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -594,20 +594,27 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
   for (const auto& cls : classes) {
     const int m_lat = std::max(cls[0], cls[1]) + 2 * b->g;
     std::vector<TileChoice> cands;
-    for (int ty = 4; ty <= tmax; ty += 2)
-      for (int tx = ty; tx <= std::min(tmax, 2 * ty); tx += ty) {
-        if (stage_smem<R>(b->h->solver, b->h->recon, b->h->de != 0, tx, ty) > smem_cap)
-          continue;
-        if (tx > m_lat || ty > m_lat) continue;
-        for (int zc : {0, 16, 32}) {
-          if (zc && zc >= cls[2]) continue;
-          TileChoice c;
-          c.tile_x = tx;
-          c.tile_y = ty;
-          c.zchunk = zc;
-          cands.push_back(c);
-        }
+    std::vector<std::pair<int, int>> shapes;
+    for (int ty : {6, 8, 10, 12, 14, 16}) {
+      for (int tx : {ty, (3 * ty) / 2, 2 * ty, 3 * ty, m_lat - 2, m_lat - 4})
+        if (tx >= ty && tx <= std::min(tmax, m_lat) && ty <= m_lat)
+          shapes.push_back({tx, ty});
+    }
+    std::sort(shapes.begin(), shapes.end());
+    shapes.erase(std::unique(shapes.begin(), shapes.end()), shapes.end());
+    for (auto& sh : shapes) {
+      if (stage_smem<R>(b->h->solver, b->h->recon, b->h->de != 0, sh.first, sh.second) >
+          smem_cap)
+        continue;
+      for (int zc : {0, 16}) {
+        if (zc && zc >= cls[2]) continue;
+        TileChoice c;
+        c.tile_x = sh.first;
+        c.tile_y = sh.second;
+        c.zchunk = zc;
+        cands.push_back(c);
       }
+    }
     float best = 1e30f;
     int rep_block = 0;
     for (int i = 0; i < b->nblocks; i++)
@@ -617,34 +624,43 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
         break;
       }
     TileChoice bestc = choice_for(b, rep_block);
-    for (const auto& c : cands) {
-      b->tune[cls] = c;
-      if (int rc = build_descriptors<R>(b, st)) {
-        cudaFree(save);
-        return rc;
+    int best_threads = b->threads;
+    for (int threads : {256, 512}) {
+      if (threads > StageThreads<R>::max) continue;
+      b->threads = threads;
+      for (const auto& c : cands) {
+        b->tune[cls] = c;
+        if (int rc = build_descriptors<R>(b, st)) {
+          cudaFree(save);
+          return rc;
+        }
+        // one untimed step, then reps timed steps
+        e = launch_stages<R>(b, st);
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch_stages<R>(b, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) break;
+        float t;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (t < best) {
+          best = t;
+          bestc = c;
+          best_threads = threads;
+        }
       }
-      // one untimed step, then reps timed steps
-      e = launch_stages<R>(b, st);
-      cudaEventRecord(e0, st);
-      for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch_stages<R>(b, st);
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
-      cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
       if (e != cudaSuccess) break;
-      float t;
-      cudaEventElapsedTime(&t, e0, e1);
-      if (t < best) {
-        best = t;
-        bestc = c;
-      }
     }
+    b->threads = best_threads;
     b->tune[cls] = bestc;
     char buf[256];
     std::snprintf(buf, sizeof(buf),
                   "%s\"%dx%dx%d\": {\"tile_x\": %d, \"tile_y\": %d, \"zchunk\": %d, "
-                  "\"ms_per_step\": %.4f, \"candidates\": %zu}",
+                  "\"threads\": %d, \"ms_per_step\": %.4f, \"candidates\": %zu}",
                   first_cls ? "" : ", ", cls[0], cls[1], cls[2], bestc.tile_x,
-                  bestc.tile_y, bestc.zchunk, best / std::max(1, reps), cands.size());
+                  bestc.tile_y, bestc.zchunk, b->threads, best / std::max(1, reps),
+                  2 * cands.size());
     json += buf;
     first_cls = false;
     if (e != cudaSuccess) break;

@@ -544,6 +544,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     info.tx = h->tile;
     info.ty = h->tile;
     info.queue = nullptr;
+    info.threads = 256;
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, tiles[i],
                         S.ntiles[i], info, h->phys, 0, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");

@@ -1,6 +1,7 @@
 // vlct_aux.cuh -- the kernels around the fused stages: the CFL timestep
 // reduction, the same-level ghost refresh gather and small copy helpers.
 #pragma once
+#include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
 #include "vlct_types.h"
 
@@ -52,6 +53,8 @@ timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
   const AuxBlock<R>& B = blocks[b];
   const size_t ncell = (size_t)B.m[0] * B.m[1] * B.m[2];
   const R g = R(phys.gamma);
+  EnergyConsts<R> econ;
+  econ.init(phys.gamma, phys.pressure_floor, DE ? phys.eta : 0.0);
   R s[3] = {R(0), R(0), R(0)};
   for (size_t c = (size_t)chunk * blockDim.x + threadIdx.x; c < ncell;
        c += (size_t)chunks_per_block * blockDim.x) {
@@ -66,40 +69,14 @@ timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
     R p;
     if (DE) {
       // apply_floor_to_energy_and_sync over the whole block (stale depth 0)
-      const double gam = phys.gamma, eta = phys.eta;
-      const float ggm1 = (float)(gam * (gam - 1.));
-      const double inv_gm1 = 1. / (gam - 1.);
-      const double half_factor = (eta != 0.) ? 0.5 : 0.;
-      const double inv_rho = 1. / (double)rho;
-      const double eint_floor = phys.pressure_floor * inv_gm1 * inv_rho;
-      const double dvx = vx, dvy = vy, dvz = vz;
-      const double v2 = (dvx * dvx + dvy * dvy + dvz * dvz);
-      double nte = 0.5 * v2, b2 = 0;
-      if (MHD) {
-        const double dbx = bx, dby = by, dbz = bz;
-        b2 = (dbx * dbx + dby * dby + dbz * dbz);
-        nte += (0.5 * b2 * inv_rho);
-      }
-      const double eint_1 = (double)B.f.c[F_ETOT][c] - nte;
-      double cur = B.f.c[F_EINT][c];
-      const double cs2_1 = fmax(0., (double)ggm1 * eint_1);
-      if ((cs2_1 > fmax(eta * v2, eta * b2 * inv_rho)) &&
-          (eint_1 > half_factor * cur))
-        cur = eint_1;
-      cur = smax(cur, eint_floor);
-      const R eint = R(cur);
+      R etot = B.f.c[F_ETOT][c], eint = B.f.c[F_EINT][c];
+      energy_floor_sync<MHD, true>(econ, rho, vx, vy, vz, bx, by, bz, etot, eint);
       B.f.c[F_EINT][c] = eint;
-      B.f.c[F_ETOT][c] = R(cur + nte);
-      p = R(phys.gamma - 1.0) * rho * eint;
+      B.f.c[F_ETOT][c] = etot;
+      p = econ.gm1 * rho * eint;
     } else {
-      const double dvx = vx, dvy = vy, dvz = vz;
-      const double ke = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-      double me = 0.;
-      if (MHD) {
-        const double dbx = bx, dby = by, dbz = bz;
-        me = 0.5 * (dbx * dbx + dby * dby + dbz * dbz);
-      }
-      p = R((phys.gamma - 1.0) * ((double)rho * ((double)B.f.c[F_ETOT][c] - ke) - me));
+      p = pressure_from_etot<R, MHD>(econ, rho, B.f.c[F_ETOT][c], vx, vy, vz, bx, by,
+                                     bz);
     }
     if (B.pressure) B.pressure[c] = p;
     R cf;
@@ -206,35 +183,36 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
       lo[a] = g;
       hi[a] = (a == face) ? g + n[a] + 1 : g + n[a];
     }
-    const long long cz = (long long)(e[2] - (hi[2] - lo[2])) * e[1] * e[0];
-    const long long cy = (long long)(hi[2] - lo[2]) * (e[1] - (hi[1] - lo[1])) * e[0];
-    const long long cx = (long long)(hi[2] - lo[2]) * (hi[1] - lo[1]) * (e[0] - (hi[0] - lo[0]));
-    const long long total = cz + cy + cx;
-    for (long long q = (long long)chunk * blockDim.x + threadIdx.x; q < total;
-         q += (long long)chunks_per_block * blockDim.x) {
+    // ghost shell = z-slabs, then y-slabs of the interior z range, then the
+    // x-ends of the interior rows (32-bit index arithmetic: a block field has
+    // far fewer than 2^31 elements)
+    const int wz = e[2] - (hi[2] - lo[2]), wy = e[1] - (hi[1] - lo[1]),
+              wx = e[0] - (hi[0] - lo[0]);
+    const int iz = hi[2] - lo[2], iy = hi[1] - lo[1];
+    const int cz = wz * e[1] * e[0];
+    const int cy = iz * wy * e[0];
+    const int cx = iz * iy * wx;
+    const int total = cz + cy + cx;
+    for (int q = chunk * blockDim.x + threadIdx.x; q < total;
+         q += chunks_per_block * blockDim.x) {
       int x, y, z;
       if (q < cz) {
-        const int w = e[2] - (hi[2] - lo[2]);
-        long long r = q;
-        x = (int)(r % e[0]); r /= e[0];
-        y = (int)(r % e[1]); r /= e[1];
-        const int zz = (int)r;
-        z = (zz < lo[2]) ? zz : zz + (hi[2] - lo[2]);
-        (void)w;
+        int r = q;
+        x = r % e[0]; r /= e[0];
+        y = r % e[1]; r /= e[1];
+        z = (r < lo[2]) ? r : r + iz;
       } else if (q < cz + cy) {
-        long long r = q - cz;
-        x = (int)(r % e[0]); r /= e[0];
-        const int wy = e[1] - (hi[1] - lo[1]);
-        const int yy = (int)(r % wy); r /= wy;
-        y = (yy < lo[1]) ? yy : yy + (hi[1] - lo[1]);
-        z = lo[2] + (int)r;
+        int r = q - cz;
+        x = r % e[0]; r /= e[0];
+        const int yy = r % wy; r /= wy;
+        y = (yy < lo[1]) ? yy : yy + iy;
+        z = lo[2] + r;
       } else {
-        long long r = q - cz - cy;
-        const int wx = e[0] - (hi[0] - lo[0]);
-        const int xx = (int)(r % wx); r /= wx;
+        int r = q - cz - cy;
+        const int xx = r % wx; r /= wx;
         x = (xx < lo[0]) ? xx : xx + (hi[0] - lo[0]);
-        y = lo[1] + (int)(r % (hi[1] - lo[1])); r /= (hi[1] - lo[1]);
-        z = lo[2] + (int)r;
+        y = lo[1] + r % iy; r /= iy;
+        z = lo[2] + r;
       }
       int idx[3] = {x, y, z}, src[3], side[3];
       for (int a = 0; a < 3; a++) {

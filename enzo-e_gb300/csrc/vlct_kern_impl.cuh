@@ -1,6 +1,8 @@
 // vlct_kern_impl.cuh -- explicit instantiation and runtime dispatch of the
 // kernel templates for one precision R.  Included once per precision TU.
 #pragma once
+#include <algorithm>
+
 #include "vlct_aux.cuh"
 #include "vlct_launch.h"
 #include "vlct_stage.cuh"
@@ -17,9 +19,18 @@ cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
   cudaError_t e = cudaFuncSetAttribute(
       k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  if (grid <= 0 || grid > nt) grid = nt;
   if (nt <= 0) return cudaSuccess;
-  k<<<grid, 256, smem, st>>>(b, t, nt, info, phys);
+  const int threads = (info.threads == 512 && StageThreads<R>::max >= 512) ? 512 : 256;
+  if (grid <= 0) {
+    // persistent grid: as many CTAs as fit on the GPU at once
+    int dev = 0, nsm = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
+    grid = std::max(1, per_sm) * nsm;
+  }
+  if (grid > nt) grid = nt;
+  k<<<grid, threads, smem, st>>>(b, t, nt, info, phys);
   return cudaGetLastError();
 }
 

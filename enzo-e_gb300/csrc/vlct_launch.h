@@ -14,7 +14,7 @@ template <class R> struct AuxBlock;
 // Largest tile extent compiled for each precision.
 template <class R> struct TileLimits;
 template <> struct TileLimits<double> { static constexpr int TMAX = 16; };
-template <> struct TileLimits<float> { static constexpr int TMAX = 24; };
+template <> struct TileLimits<float> { static constexpr int TMAX = 40; };
 
 template <class R>
 cudaError_t launch_stage(int solver, int recon, bool de,

@@ -26,6 +26,7 @@
 // (total minus kinetic minus magnetic energy) and the energy floor / sync run
 // in FP64.
 #pragma once
+#include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
 #include "vlct_types.h"
 
@@ -39,6 +40,18 @@ enum { S_RHO = 0, S_MX = 1, S_E = 4, S_BJ = 5, S_BK = 6, S_EINT = 7, S_VBAR = 8 
 __device__ __forceinline__ bool inr(int a, int lo, int hi) {
   return a >= lo && a < hi;
 }
+
+// Division by a runtime divisor d < 2^16 of a numerator n < 2^16, by a
+// multiply-high with ceil(2^32 / d) (exact because n * d < 2^32).
+struct FastDiv {
+  unsigned d, m;
+  // ceil(2^32 / d) == floor((2^32 - 1) / d) + 1 for every d > 1
+  __device__ __forceinline__ explicit FastDiv(unsigned dd)
+      : d(dd), m(dd > 1 ? 0xFFFFFFFFu / dd + 1u : 0u) {}
+  __device__ __forceinline__ int div(int n) const {
+    return d > 1 ? (int)__umulhi((unsigned)n, m) : n;
+  }
+};
 
 // Upwind weight of CT from the sign of the density flux
 // (EnzoBfieldMethodCT.cpp:198-213).
@@ -64,7 +77,9 @@ __device__ __forceinline__ R edge_emf(R Ej, R Ej_kp1, R Ek, R Ek_jp1, R Wj,
 template <class R, int SOLVER, int RECON, bool DE> struct StageCfg {
   static constexpr bool MHD = SOLVER != SOLVER_HLLC;
   static constexpr int LOOK = (RECON == RECON_NN) ? 1 : 2;
-  static constexpr int NRING = 2 * LOOK;
+  // ring of primitive planes: the planes a step reads plus the plane loaded
+  // ahead for the next step
+  static constexpr int NRING = (RECON == RECON_NN) ? 3 : 4;
   static constexpr int RP = (RECON == RECON_NN) ? 0 : 1;
   static constexpr int NF = DE ? 9 : (MHD ? 7 : 5);
 };
@@ -87,7 +102,7 @@ struct SmemLayout {
     o_xf = o; o += 2 * nf * G;
     o_yf = o; o += 2 * nf * G;
     o_zf = o; o += 2 * nf * G;
-    o_ec = o; o += 2 * 3 * G;
+    o_ec = o; o += nring * 3 * G;
     o_ex = o; o += 2 * G;
     o_ey = o; o += 2 * G;
     o_ez = o; o += G;
@@ -106,8 +121,14 @@ size_t stage_smem_bytes(int tx, int ty) {
   return (size_t)L.total * sizeof(R);
 }
 
+// FP32: launched with 256 or 512 threads (the tuner's choice), registers
+// capped at 128 so that a 512-thread CTA fits an SM.  FP64: 256 threads with
+// up to 255 registers (the FP64 solver does not fit in 128 without spilling).
+template <class R> struct StageThreads { static constexpr int max = 256; };
+template <> struct StageThreads<float> { static constexpr int max = 512; };
+
 template <class R, int SOLVER, int RECON, bool DE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(StageThreads<R>::max, 1)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
              const StageTile* __restrict__ tiles, int ntiles, StageInfo info,
              PhysParams phys) {
@@ -119,6 +140,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   SmemLayout Ls;
   Ls.init(info.tx, info.ty, RP, NRING, NF);
   const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;
+  const int PQ = PP * QP;
   R* s_prim = sm + Ls.o_prim;
   R* s_xf = sm + Ls.o_xf;
   R* s_yf = sm + Ls.o_yf;
@@ -135,8 +157,12 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   const R g = R(phys.gamma);
   const R theta = R(phys.theta_limiter);
   const R dfloor = R(phys.density_floor), pfloor = R(phys.pressure_floor);
+  EnergyConsts<R> econ;
+  econ.init(phys.gamma, phys.pressure_floor, DE ? phys.eta : 0.0);
+  const FastDiv divPP(Ls.PP), divHP(Ls.HP);
 
   __shared__ int s_next;
+  __shared__ R s_dtdx[3];
   int it = blockIdx.x;
   if (info.queue) {
     if (tid == 0) s_next = atomicAdd(info.queue, 1);
@@ -149,13 +175,19 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
     const int xa = tl.xa, xb = tl.xb, ya = tl.ya, yb = tl.yb;
     const int tx = xb - xa, ty = yb - ya;
-    const double dt = *B.dt * info.dt_factor;
-    const R dtdx[3] = {R(dt / B.cw[0]), R(dt / B.cw[1]), R(dt / B.cw[2])};
+    // dt / dx per axis, once per tile (FP64 divisions: one thread)
+    if (tid == 0) {
+      const double dt = *B.dt * info.dt_factor;
+      s_dtdx[0] = R(dt / B.cw[0]);
+      s_dtdx[1] = R(dt / B.cw[1]);
+      s_dtdx[2] = R(dt / B.cw[2]);
+    }
+    __syncthreads();
+    const R dtdx[3] = {s_dtdx[0], s_dtdx[1], s_dtdx[2]};
     // output window of centred B (and the z-march range)
     const int olo = info.final_stage ? S : S + 1;
     const int ohi_x = info.final_stage ? m0 - S : m0 - S - 1;
     const int ohi_y = info.final_stage ? m1 - S : m1 - S - 1;
-    const int ohi_z = info.final_stage ? m2 - S : m2 - S - 1;
     const int za = tl.za, zb = tl.zb;  // output planes of this chunk
     const int t0 = za - 1;
     // prim-tile origin and halo-grid origin
@@ -163,17 +195,18 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     const int hx0 = xa - 1, hy0 = ya - 1;
     const size_t cstr_y = (size_t)m0, cstr_z = (size_t)m0 * m1;
 
-    auto prim_at = [&](int slot, int q, int x, int y) -> R& {
-      return s_prim[((slot * NQ + q) * QP + (y - py0)) * PP + (x - px0)];
+    // offset of cell (x, y) of ring slot `slot` in s_prim (add q * PQ)
+    auto poff = [&](int slot, int x, int y) -> int {
+      return slot * NQ * PQ + (y - py0) * PP + (x - px0);
     };
 
-    // ---- phase A: primitives of plane p into ring slot p % NRING --------
+    // ---- primitives (and the cell-centred E) of plane p into its ring slot
     auto load_plane = [&](int p) {
       if (!inr(p, s, m2 - s)) return;
       const int slot = p % NRING;
-      const double gm1 = phys.gamma - 1.0;
-      for (int idx = tid; idx < PP * QP; idx += nthr) {
-        const int x = px0 + idx % PP, y = py0 + idx / PP;
+      for (int idx = tid; idx < PQ; idx += nthr) {
+        const int qy = divPP.div(idx);
+        const int x = px0 + (idx - qy * PP), y = py0 + qy;
         if (!inr(x, s, m0 - s) || !inr(y, s, m1 - s)) continue;
         const size_t c = (size_t)p * cstr_z + (size_t)y * cstr_y + x;
         const R rho = B.cur.c[F_RHO][c];
@@ -187,149 +220,28 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         R p_out;
         // EnzoComputePressure::compute_pressure (EnzoComputePressure.cpp:127-190)
         if (DE) {
-          p_out = R(gm1) * rho * B.cur.c[F_EINT][c];
+          p_out = econ.gm1 * rho * B.cur.c[F_EINT][c];
         } else {
-          // total minus kinetic minus magnetic energy: FP64 in both forms
-          const double dvx = vx, dvy = vy, dvz = vz;
-          const double ke = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-          double me = 0.;
-          if (MHD) {
-            const double dbx = bx, dby = by, dbz = bz;
-            me = 0.5 * (dbx * dbx + dby * dby + dbz * dbz);
-          }
-          p_out = R(gm1 * ((double)rho * ((double)B.cur.c[F_ETOT][c] - ke) - me));
+          p_out = pressure_from_etot<R, MHD>(econ, rho, B.cur.c[F_ETOT][c], vx, vy, vz,
+                                             bx, by, bz);
         }
-        prim_at(slot, Q_RHO, x, y) = rho;
-        prim_at(slot, Q_VX + 0, x, y) = vx;
-        prim_at(slot, Q_VX + 1, x, y) = vy;
-        prim_at(slot, Q_VX + 2, x, y) = vz;
+        R* w = s_prim + poff(slot, x, y);
+        w[Q_RHO * PQ] = rho;
+        w[(Q_VX + 0) * PQ] = vx;
+        w[(Q_VX + 1) * PQ] = vy;
+        w[(Q_VX + 2) * PQ] = vz;
         if (MHD) {
-          prim_at(slot, Q_BX + 0, x, y) = bx;
-          prim_at(slot, Q_BX + 1, x, y) = by;
-          prim_at(slot, Q_BX + 2, x, y) = bz;
+          w[(Q_BX + 0) * PQ] = bx;
+          w[(Q_BX + 1) * PQ] = by;
+          w[(Q_BX + 2) * PQ] = bz;
         }
-        prim_at(slot, Q_P, x, y) = p_out;
-      }
-    };
-
-    // Reconstructed L/R primitives of one face (face frame) along dim d.
-    // w(k) returns the primitive q at the k-th cell along d (k = -1..2 around
-    // the face between cells 0 and 1).
-    auto reconstruct = [&](int d, auto&& w, R* wl, R* wr) {
-      const int qmap[8] = {Q_RHO, Q_BX + d, Q_BX + (d + 1) % 3, Q_BX + (d + 2) % 3,
-                           Q_VX + d, Q_VX + (d + 1) % 3, Q_VX + (d + 2) % 3, Q_P};
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        if (!MHD && (k == L_BI || k == L_BJ || k == L_BK)) {
-          wl[k] = wr[k] = R(0);
-          continue;
-        }
-        const int q = qmap[k];
-        if (RECON == RECON_NN) {
-          wl[k] = w(q, 0);
-          wr[k] = w(q, 1);
-        } else {
-          const R a = w(q, -1), b0 = w(q, 0), b1 = w(q, 1), c = w(q, 2);
-          R dl, dr;
-          if (RECON == RECON_PLM) {
-            dl = limiter_enzo_rk(a, b0, b1, theta);
-            dr = limiter_enzo_rk(b0, b1, c, theta);
-          } else {
-            dl = limiter_athena(a, b0, b1);
-            dr = limiter_athena(b0, b1, c);
-          }
-          const R hl = dl * R(0.5), hr = dr * R(0.5);
-          R lv = b0 + hl, rv = b1 - hr;
-          if (q == Q_RHO) {
-            lv = smax(lv, dfloor);
-            rv = smax(rv, dfloor);
-          } else if (q == Q_P) {
-            lv = smax(lv, pfloor);
-            rv = smax(rv, pfloor);
-          }
-          wl[k] = lv;
-          wr[k] = rv;
-        }
-      }
-    };
-
-    // Solve one face and store its fluxes (global component order).
-    auto solve_store = [&](int d, R* wl, R* wr, R* dst) {
-      FaceFlux<R> F;
-      riemann<SOLVER, R>(g, wl, wr, F);
-      dst[S_RHO * G] = F.f[L_RHO];
-      dst[(S_MX + d) * G] = F.f[L_VI];
-      dst[(S_MX + (d + 1) % 3) * G] = F.f[L_VJ];
-      dst[(S_MX + (d + 2) % 3) * G] = F.f[L_VK];
-      dst[S_E * G] = F.f[L_E];
-      if (MHD) {
-        dst[S_BJ * G] = F.f[L_BJ];
-        dst[S_BK * G] = F.f[L_BK];
-      }
-      if (DE) {
-        dst[S_EINT * G] = F.eflux;
-        dst[S_VBAR * G] = F.vbar;
-      }
-    };
-
-    // ---- phase B items for step t: z-faces at t+1/2, x/y faces and
-    // cell-centred E of plane t+1 (the prologue runs the plane part only).
-    auto phase_b = [&](int t, bool zfaces, int pl) {
-      const bool plane_ok = inr(pl, S, m2 - S);
-      const int nitem = 4 * G;
-      for (int idx = tid; idx < nitem; idx += nthr) {
-        const int kind = idx / G, r = idx - kind * G;
-        const int i = r % HP, j = r / HP;
-        const int x = hx0 + i, y = hy0 + j;
-        R wl[8], wr[8];
-        if (kind == 0) {  // z-face fz = t (between planes t and t+1)
-          const int fz = t;
-          if (!zfaces || !inr(fz, S, m2 - 1 - S) || !inr(x, S, m0 - S) ||
-              !inr(y, S, m1 - S))
-            continue;
-          reconstruct(2, [&](int q, int k) -> R {
-            return prim_at((fz + k + NRING) % NRING, q, x, y);
-          }, wl, wr);
-          if (MHD) {  // correct_reconstructed_bfield (EnzoBfieldMethodCT.cpp:122-166)
-            const R bf = B.cur.f[2][(size_t)(fz + 1) * cstr_z + (size_t)y * cstr_y + x];
-            wl[L_BI] = bf;
-            wr[L_BI] = bf;
-          }
-          solve_store(2, wl, wr, s_zf + (size_t)(fz & 1) * NF * G + r);
-        } else if (kind == 1) {  // x-face fx = x of plane pl
-          if (i > tx || !plane_ok || !inr(x, S, m0 - 1 - S) || !inr(y, S, m1 - S))
-            continue;
-          const int slot = pl % NRING;
-          reconstruct(0, [&](int q, int k) -> R { return prim_at(slot, q, x + k, y); },
-                      wl, wr);
-          if (MHD) {
-            const R bf = B.cur.f[0][(size_t)pl * (m1 * (size_t)(m0 + 1)) +
-                                    (size_t)y * (m0 + 1) + (x + 1)];
-            wl[L_BI] = bf;
-            wr[L_BI] = bf;
-          }
-          solve_store(0, wl, wr, s_xf + (size_t)(pl & 1) * NF * G + r);
-        } else if (kind == 2) {  // y-face fy = y of plane pl
-          if (j > ty || !plane_ok || !inr(y, S, m1 - 1 - S) || !inr(x, S, m0 - S))
-            continue;
-          const int slot = pl % NRING;
-          reconstruct(1, [&](int q, int k) -> R { return prim_at(slot, q, x, y + k); },
-                      wl, wr);
-          if (MHD) {
-            const R bf = B.cur.f[1][(size_t)pl * ((size_t)(m1 + 1) * m0) +
-                                    (size_t)(y + 1) * m0 + x];
-            wl[L_BI] = bf;
-            wr[L_BI] = bf;
-          }
-          solve_store(1, wl, wr, s_yf + (size_t)(pl & 1) * NF * G + r);
-        } else {  // cell-centred E (EnzoBfieldMethodCT.cpp:267-292)
-          if (!MHD || !plane_ok || !inr(x, S, m0 - S) || !inr(y, S, m1 - S)) continue;
-          const int slot = pl % NRING;
-          const R vx = prim_at(slot, Q_VX, x, y), vy = prim_at(slot, Q_VX + 1, x, y),
-                  vz = prim_at(slot, Q_VX + 2, x, y);
-          const R bx = prim_at(slot, Q_BX, x, y), by = prim_at(slot, Q_BX + 1, x, y),
-                  bz = prim_at(slot, Q_BX + 2, x, y);
-          R* e = s_ec + (size_t)(pl & 1) * 3 * G + r;
+        w[Q_P * PQ] = p_out;
+        // cell-centred E = -v x B (EnzoBfieldMethodCT.cpp:267-292), on the
+        // halo grid and inside [S, m - S)
+        const int hi = x - hx0, hj = y - hy0;
+        if (MHD && hi >= 0 && hi < HP && hj >= 0 && hj < Ls.HQ &&
+            inr(x, S, m0 - S) && inr(y, S, m1 - S) && inr(p, S, m2 - S)) {
+          R* e = s_ec + slot * 3 * G + hj * HP + hi;
           e[0] = (-vy * bz + vz * by);
           e[G] = (-vz * bx + vx * bz);
           e[2 * G] = (-vx * by + vy * bx);
@@ -337,17 +249,130 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
       }
     };
 
+    // ---- Riemann solves: z-faces at t+1/2 (if zfaces) and the x- and
+    // y-faces of plane pl.  One code path for all three directions.
+    auto phase_b = [&](int t, bool zfaces, int pl) {
+      const int HQv = Ls.HQ;
+      const FastDiv divX(tx + 1);
+      const int nz = zfaces ? HP * HQv : 0;
+      const int nx = (tx + 1) * HQv;
+      const int ny = HP * (ty + 1);
+      const bool plane_ok = inr(pl, S, m2 - S);
+      for (int idx = tid; idx < nz + nx + ny; idx += nthr) {
+        int d, i, j;
+        if (idx < nz) {
+          d = 2; j = divHP.div(idx); i = idx - j * HP;
+        } else if (idx < nz + nx) {
+          const int q = idx - nz;
+          d = 0; j = divX.div(q); i = q - j * (tx + 1);
+        } else {
+          const int q = idx - nz - nx;
+          d = 1; j = divHP.div(q); i = q - j * HP;
+        }
+        const int x = hx0 + i, y = hy0 + j;
+        // face index f along d: the face between cells f and f+1
+        int off[4];  // s_prim offsets of the cells f-1 .. f+2 along d
+        const R* bface;
+        R* dst;
+        const int r = j * HP + i;
+        if (d == 2) {
+          const int fz = t;
+          if (!inr(fz, S, m2 - 1 - S) || !inr(x, S, m0 - S) || !inr(y, S, m1 - S))
+            continue;
+#pragma unroll
+          for (int k = 0; k < 4; k++) off[k] = poff((fz - 1 + k + NRING) % NRING, x, y);
+          bface = B.cur.f[2] + ((size_t)(fz + 1) * cstr_z + (size_t)y * cstr_y + x);
+          dst = s_zf + (size_t)(fz & 1) * NF * G + r;
+        } else {
+          if (!plane_ok) continue;
+          const int slot = pl % NRING;
+          if (d == 0) {
+            if (!inr(x, S, m0 - 1 - S) || !inr(y, S, m1 - S)) continue;
+#pragma unroll
+            for (int k = 0; k < 4; k++) off[k] = poff(slot, x - 1 + k, y);
+            bface = B.cur.f[0] + ((size_t)pl * ((size_t)m1 * (m0 + 1)) +
+                                  (size_t)y * (m0 + 1) + (x + 1));
+            dst = s_xf + (size_t)(pl & 1) * NF * G + r;
+          } else {
+            if (!inr(y, S, m1 - 1 - S) || !inr(x, S, m0 - S)) continue;
+#pragma unroll
+            for (int k = 0; k < 4; k++) off[k] = poff(slot, x, y - 1 + k);
+            bface = B.cur.f[1] + ((size_t)pl * ((size_t)(m1 + 1) * m0) +
+                                  (size_t)(y + 1) * m0 + x);
+            dst = s_yf + (size_t)(pl & 1) * NF * G + r;
+          }
+        }
+        // reconstruction (EnzoReconstructorNN.cpp:14-49,
+        // EnzoReconstructorPLM.hpp:167-345), in the face frame
+        R wl[8], wr[8];
+        const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          if (!MHD && (k == L_BI || k == L_BJ || k == L_BK)) {
+            wl[k] = wr[k] = R(0);
+            continue;
+          }
+          const int q = (k == L_RHO) ? Q_RHO
+                      : (k == L_BI) ? Q_BX + d : (k == L_BJ) ? Q_BX + d1
+                      : (k == L_BK) ? Q_BX + d2 : (k == L_VI) ? Q_VX + d
+                      : (k == L_VJ) ? Q_VX + d1 : (k == L_VK) ? Q_VX + d2 : Q_P;
+          const R* w = s_prim + q * PQ;
+          if (RECON == RECON_NN) {
+            wl[k] = w[off[1]];
+            wr[k] = w[off[2]];
+          } else {
+            const R a = w[off[0]], b0 = w[off[1]], b1 = w[off[2]], c = w[off[3]];
+            R dl, dr;
+            if (RECON == RECON_PLM) {
+              dl = limiter_enzo_rk(a, b0, b1, theta);
+              dr = limiter_enzo_rk(b0, b1, c, theta);
+            } else {
+              dl = limiter_athena(a, b0, b1);
+              dr = limiter_athena(b0, b1, c);
+            }
+            R lv = b0 + dl * R(0.5), rv = b1 - dr * R(0.5);
+            if (k == L_RHO) {
+              lv = smax(lv, dfloor);
+              rv = smax(rv, dfloor);
+            } else if (k == L_E) {
+              lv = smax(lv, pfloor);
+              rv = smax(rv, pfloor);
+            }
+            wl[k] = lv;
+            wr[k] = rv;
+          }
+        }
+        if (MHD) {  // correct_reconstructed_bfield (EnzoBfieldMethodCT.cpp:122-166)
+          const R bf = *bface;
+          wl[L_BI] = bf;
+          wr[L_BI] = bf;
+        }
+        FaceFlux<R> F;
+        riemann<SOLVER, R>(g, wl, wr, F);
+        dst[S_RHO * G] = F.f[L_RHO];
+        dst[(S_MX + d) * G] = F.f[L_VI];
+        dst[(S_MX + d1) * G] = F.f[L_VJ];
+        dst[(S_MX + d2) * G] = F.f[L_VK];
+        dst[S_E * G] = F.f[L_E];
+        if (MHD) {
+          dst[S_BJ * G] = F.f[L_BJ];
+          dst[S_BK * G] = F.f[L_BK];
+        }
+        if (DE) {
+          dst[S_EINT * G] = F.eflux;
+          dst[S_VBAR * G] = F.vbar;
+        }
+      }
+    };
+
     // ---------------------------------------------------------- prologue --
-    for (int p = t0 - (LOOK - 1); p <= t0 + LOOK - 1; p++) load_plane(p);
+    for (int p = t0 - (LOOK - 1); p <= t0 + LOOK; p++) load_plane(p);
     __syncthreads();
     phase_b(t0 - 1, false, t0);
     __syncthreads();
 
     for (int t = t0; t < zb; t++) {
-      // ---- A
-      load_plane(t + LOOK);
-      __syncthreads();
-      // ---- B
+      // ---- B: z-faces at t+1/2, x/y faces of plane t+1
       phase_b(t, true, t + 1);
       __syncthreads();
       // ---- C: edge EMFs (EnzoBfieldMethodCT.cpp:480-590)
@@ -357,11 +382,11 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         const R* yf0 = s_yf + (size_t)(t & 1) * NF * G;
         const R* yf1 = s_yf + (size_t)((t + 1) & 1) * NF * G;
         const R* zf = s_zf + (size_t)(t & 1) * NF * G;
-        const R* ec0 = s_ec + (size_t)(t & 1) * 3 * G;
-        const R* ec1 = s_ec + (size_t)((t + 1) & 1) * 3 * G;
+        const R* ec0 = s_ec + (size_t)(t % NRING) * 3 * G;
+        const R* ec1 = s_ec + (size_t)((t + 1) % NRING) * 3 * G;
         for (int idx = tid; idx < 3 * G; idx += nthr) {
-          const int kind = idx / G, r = idx - kind * G;
-          const int i = r % HP, j = r / HP;
+          const int kind = idx < G ? 0 : (idx < 2 * G ? 1 : 2), r = idx - kind * G;
+          const int j = divHP.div(r), i = r - j * HP;
           const int x = hx0 + i, y = hy0 + j;
           if (kind == 0) {  // E_x at (x, y+1/2, t+1/2)
             if (i < 1 || i > tx || j > ty) continue;
@@ -395,14 +420,17 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           }
         }
         __syncthreads();
-        // ---- D1: face updates (EnzoBfieldMethodCT.cpp:617-687); a face that
-        // is not updated in this stage keeps its start-of-step value.
+      }
+      // ---- D1: face updates (EnzoBfieldMethodCT.cpp:617-687); a face that
+      // is not updated in this stage keeps its start-of-step value.  The
+      // primitives of plane t+1+LOOK (next step) load in the same phase.
+      if (MHD) {
         const bool do_plane = t >= za;
         // the lowest face of a chunk is written by the chunk below it
         const bool own_bz = t >= za || za == olo;
         for (int idx = tid; idx < 3 * G; idx += nthr) {
-          const int kind = idx / G, r = idx - kind * G;
-          const int i = r % HP, j = r / HP;
+          const int kind = idx < G ? 0 : (idx < 2 * G ? 1 : 2), r = idx - kind * G;
+          const int j = divHP.div(r), i = r - j * HP;
           const int x = hx0 + i, y = hy0 + j;
           if (kind == 0) {  // Bz at face kz = t+1 of column (x, y)
             if (i < 1 || i > tx || j < 1 || j > ty) continue;
@@ -460,6 +488,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           }
         }
       }
+      if (t + 1 < zb) load_plane(t + 1 + LOOK);
       __syncthreads();
       // ---- D2: cell updates of plane t
       if (t >= za) {
@@ -468,8 +497,10 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         const R* zfm = s_zf + (size_t)((t - 1) & 1) * NF * G;
         const R* zfp = s_zf + (size_t)(t & 1) * NF * G;
         const int slot = t % NRING;
+        const FastDiv divT(tx);
         for (int idx = tid; idx < tx * ty; idx += nthr) {
-          const int x = xa + idx % tx, y = ya + idx / tx;
+          const int qy = divT.div(idx);
+          const int x = xa + (idx - qy * tx), y = ya + qy;
           const int r = (y - hy0) * HP + (x - hx0);
           const size_t c = (size_t)t * cstr_z + (size_t)y * cstr_y + x;
           const bool in_out = x < ohi_x && y < ohi_y;
@@ -498,7 +529,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
             du[k] = a;
           }
           if (DE) {
-            const R p = smax(prim_at(slot, Q_P, x, y), pfloor);
+            const R p = smax(s_prim[poff(slot, x, y) + Q_P * PQ], pfloor);
             R a = R(0.0);
             a -= dtdx[0] * (xf0[S_EINT * G + r] - xf0[S_EINT * G + r - 1]);
             a -= dtdx[0] * p * (xf0[S_VBAR * G + r] - xf0[S_VBAR * G + r - 1]);
@@ -519,40 +550,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           R etot = (B.base.c[F_ETOT][c] * old_rho + du[4]) * inv_new_rho;
           R eint = R(0);
           if (DE) eint = (B.base.c[F_EINT][c] * old_rho + du[5]) * inv_new_rho;
-          // apply_floor_to_energy_and_sync (EnzoPhysicsFluidProps.cpp:162-290),
-          // evaluated in FP64
-          {
-            const double gam = phys.gamma;
-            const double eta = DE ? phys.eta : 0.0;
-            const float ggm1 = (float)(gam * (gam - 1.));
-            const double inv_gm1 = 1. / (gam - 1.);
-            const double half_factor = (eta != 0.) ? 0.5 : 0.;
-            const double inv_rho = 1. / (double)new_rho;
-            const double eint_floor = phys.pressure_floor * inv_gm1 * inv_rho;
-            const double dvx = vx, dvy = vy, dvz = vz;
-            const double v2 = (dvx * dvx + dvy * dvy + dvz * dvz);
-            double nte = 0.5 * v2;
-            double b2 = 0;
-            if (MHD) {
-              const double dbx = bcx, dby = bcy, dbz = bcz;
-              b2 = (dbx * dbx + dby * dby + dbz * dbz);
-              nte += (0.5 * b2 * inv_rho);
-            }
-            if (DE) {
-              const double eint_1 = (double)etot - nte;
-              double cur = eint;
-              const double cs2_1 = fmax(0., (double)ggm1 * eint_1);
-              if ((cs2_1 > fmax(eta * v2, eta * b2 * inv_rho)) &&
-                  (eint_1 > half_factor * cur))
-                cur = eint_1;
-              cur = smax(cur, eint_floor);
-              eint = R(cur);
-              etot = R(cur + nte);
-            } else {
-              const double etot_floor = eint_floor + nte;
-              etot = R(smax((double)etot, etot_floor));
-            }
-          }
+          // apply_floor_to_energy_and_sync (EnzoPhysicsFluidProps.cpp:162-290)
+          energy_floor_sync<MHD, DE>(econ, new_rho, vx, vy, vz, bcx, bcy, bcz, etot,
+                                     eint);
           B.out.c[F_RHO][c] = new_rho;
           B.out.c[F_VX][c] = vx;
           B.out.c[F_VY][c] = vy;

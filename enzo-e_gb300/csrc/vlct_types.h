@@ -51,6 +51,7 @@ struct StageInfo {
   int tx, ty;       // maximum tile extent of the launch (sizes shared memory)
   int* queue;       // work counter (zeroed before the launch) for a persistent
                     // grid pulling tiles dynamically; null = static grid stride
+  int threads;      // CTA size (256 or 512); 0 = 256
 };
 
 }  // namespace vlct
