@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "capi_internal.h"
@@ -637,4 +638,219 @@ extern "C" int mhdvlct_fill_ghosts_periodic(mhdvlct_handle* h, const MhdBlockVie
   cudaStream_t st = (cudaStream_t)stream;
   return b->dtype == MHD_DTYPE_F64 ? fill_ghosts_t<double>(h, b, st)
                                    : fill_ghosts_t<float>(h, b, st);
+}
+
+// ------------------------------------------------ no-allocation block step
+// mhdvlct_block_step_noalloc: the plain block step with its device scratch
+// in one file-scope array instead of a cudaMalloc'd buffer.  Nothing in this
+// section calls cudaMalloc, cudaFree or any other allocating routine; the
+// device address of the array is looked up once per device with
+// cudaGetSymbolAddress and cached.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB per device
+constexpr int kNoAllocMaxTiles = 512;                     // per stage
+constexpr int kNoAllocMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+char* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device (first call per
+// device resolves it; later calls read the cache).
+int noalloc_base(mhdvlct_handle* h, char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(h, MHD_ERR_INVALID, "device ordinal beyond the no-alloc scratch table");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(no-alloc scratch)");
+    g_noalloc_base[dev] = (char*)p;
+  }
+  *out = g_noalloc_base[dev];
+  return MHD_OK;
+}
+
+// The tiles make_tiles produces (same order, same near-equal split), written
+// into a caller array of capacity `cap`; returns the count, or -1 past cap.
+int noalloc_tiles(const int m[3], int S, bool final, int tx, int ty, int zchunk,
+                  StageTile* out, int cap) {
+  const int lo = final ? S : S + 1;
+  const int hi[3] = {final ? m[0] - S : m[0] - S - 1, final ? m[1] - S : m[1] - S - 1,
+                     final ? m[2] - S : m[2] - S - 1};
+  int len[3], t[3] = {tx, ty, 0}, np[3];
+  t[2] = zchunk > 0 ? zchunk : (hi[2] - lo);
+  for (int a = 0; a < 3; a++) {
+    len[a] = hi[a] - lo;
+    if (len[a] <= 0) return 0;
+    if (t[a] <= 0 || t[a] > len[a]) t[a] = len[a];
+    np[a] = (len[a] + t[a] - 1) / t[a];
+  }
+  if ((long long)np[0] * np[1] * np[2] > cap) return -1;
+  auto part = [&](int a, int i, int& p0, int& p1) {
+    p0 = lo;
+    for (int j = 0; j < i; j++) p0 += len[a] / np[a] + (j < len[a] % np[a] ? 1 : 0);
+    p1 = p0 + len[a] / np[a] + (i < len[a] % np[a] ? 1 : 0);
+  };
+  int n = 0;
+  for (int k = 0; k < np[2]; k++)
+    for (int j = 0; j < np[1]; j++)
+      for (int i = 0; i < np[0]; i++) {
+        StageTile& T = out[n++];
+        T.block = 0;
+        part(0, i, T.xa, T.xb);
+        part(1, j, T.ya, T.yb);
+        part(2, k, T.za, T.zb);
+      }
+  return n;
+}
+
+template <class R>
+int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
+                         cudaStream_t st) {
+  const int g = b->ghost[0];
+  const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
+  const StagePlan sp = stage_plan(h);
+  if (h->tile <= 0) h->tile = 8;
+
+  // the tile lists live on the host stack, bounded by kNoAllocMaxTiles
+  StageTile tiles[2][kNoAllocMaxTiles];
+  int ntiles[2] = {0, 0};
+  for (int i = 0; i < sp.nstages; i++) {
+    ntiles[i] = noalloc_tiles(m, sp.S[i], i + 1 == sp.nstages, h->tile, h->tile,
+                              h->zchunk, tiles[i], kNoAllocMaxTiles);
+    if (ntiles[i] < 0)
+      return fail(h, MHD_ERR_INVALID,
+                  "block needs more than " + std::to_string(kNoAllocMaxTiles) +
+                      " tiles per stage; mhdvlct_block_step_noalloc cannot take it "
+                      "(use mhdvlct_block_step)");
+  }
+
+  // carve the static array: cells, stage-0 faces, final faces, dt, stage
+  // descriptors, tiles (each region 256-byte aligned)
+  const size_t M = (size_t)m[0] * m[1] * m[2];
+  const size_t F[3] = {(size_t)(m[0] + 1) * m[1] * m[2], (size_t)m[0] * (m[1] + 1) * m[2],
+                       (size_t)m[0] * m[1] * (m[2] + 1)};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += align_up(bytes);
+    return o;
+  };
+  size_t o_tmp[NCELL], o_tf[3], o_ff[3];
+  for (int k = 0; k < NCELL; k++) o_tmp[k] = take(M * sizeof(R));
+  for (int d = 0; d < 3; d++) o_tf[d] = take(F[d] * sizeof(R));
+  for (int d = 0; d < 3; d++) o_ff[d] = take(F[d] * sizeof(R));
+  const size_t o_dt = take(sizeof(double));
+  const size_t o_sb = take(2 * sizeof(StageBlock<R>));
+  const size_t o_tl = take((size_t)(ntiles[0] + ntiles[1]) * sizeof(StageTile));
+  if (off > kNoAllocScratchBytes)
+    return fail(h, MHD_ERR_INVALID,
+                "block needs " + std::to_string(off) +
+                    " bytes of scratch; mhdvlct_block_step_noalloc holds at most " +
+                    std::to_string(kNoAllocScratchBytes) +
+                    " bytes (use mhdvlct_block_step)");
+
+  char* base = nullptr;
+  int rc = noalloc_base(h, &base);
+  if (rc) return rc;
+  PlainScratch<R> S;
+  for (int k = 0; k < NCELL; k++) S.tmp[k] = (R*)(base + o_tmp[k]);
+  for (int d = 0; d < 3; d++) {
+    S.tface[d] = (R*)(base + o_tf[d]);
+    S.fface[d] = (R*)(base + o_ff[d]);
+  }
+  S.d_dt = (double*)(base + o_dt);
+  S.d_sblocks = (StageBlock<R>*)(base + o_sb);
+  S.d_tiles = (StageTile*)(base + o_tl);
+
+  FieldSet<R> ext = fieldset_of<R>(b);
+  FieldSet<R> tmp;
+  for (int k = 0; k < NCELL; k++) tmp.c[k] = S.tmp[k];
+  for (int d = 0; d < 3; d++) tmp.f[d] = S.tface[d];
+  cudaError_t e = launch_set_scalar(S.d_dt, dt, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "dt upload");
+
+  StageBlock<R> sb[2];
+  for (int i = 0; i < sp.nstages; i++) {
+    StageBlock<R>& B = sb[i];
+    for (int a = 0; a < 3; a++) {
+      B.m[a] = m[a];
+      B.cw[a] = b->cell_width[a];
+    }
+    B.dt = S.d_dt;
+    B.base = ext;
+    if (sp.nstages == 1) {
+      B.cur = tmp;
+      for (int d = 0; d < 3; d++) B.cur.f[d] = ext.f[d];
+      B.out = ext;
+    } else if (i == 0) {
+      B.cur = ext;
+      B.out = tmp;
+    } else {
+      B.cur = tmp;
+      B.out = ext;
+    }
+    if (i + 1 == sp.nstages)
+      for (int d = 0; d < 3; d++) B.out.f[d] = S.fface[d];
+  }
+  e = cudaMemcpyAsync(S.d_sblocks, sb, sizeof(sb), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "block upload");
+  if (ntiles[0] > 0) {
+    e = cudaMemcpyAsync(S.d_tiles, tiles[0], ntiles[0] * sizeof(StageTile),
+                        cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "tile upload");
+  }
+  if (ntiles[1] > 0) {
+    e = cudaMemcpyAsync(S.d_tiles + ntiles[0], tiles[1], ntiles[1] * sizeof(StageTile),
+                        cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "tile upload");
+  }
+  if (sp.nstages == 1) {
+    for (int k = 0; k < NCELL; k++) {
+      if (!ext.c[k]) continue;
+      e = cudaMemcpyAsync(S.tmp[k], ext.c[k], M * sizeof(R), cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
+    }
+  }
+  const StageTile* dtiles[2] = {S.d_tiles, S.d_tiles + ntiles[0]};
+  for (int i = 0; i < sp.nstages; i++) {
+    StageInfo info;
+    info.s = sp.s[i];
+    info.S = sp.S[i];
+    info.final_stage = (i + 1) == sp.nstages;
+    info.dt_factor = sp.dt_factor[i];
+    info.tx = h->tile;
+    info.ty = h->tile;
+    info.queue = nullptr;
+    info.threads = 256;
+    e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, dtiles[i],
+                        ntiles[i], info, h->phys, 0, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");
+  }
+  if (h->mhd) {
+    const int S1 = sp.S[sp.nstages - 1] + 1;
+    e = launch_copy_faces<R>(m[0], m[1], m[2], S1, S.fface[0], S.fface[1], S.fface[2],
+                             ext.f[0], ext.f[1], ext.f[2], st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "face copy");
+  }
+  return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" int mhdvlct_block_step_noalloc(mhdvlct_handle* h, const MhdBlockView* b,
+                                          double dt, void* stream) {
+  if (!h) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? block_step_noalloc_t<double>(h, b, dt, st)
+                                   : block_step_noalloc_t<float>(h, b, dt, st);
 }

@@ -28,6 +28,7 @@ EXPORTED = (
     "mhdvlct_params_default", "mhdvlct_params_parse", "mhdvlct_create",
     "mhdvlct_destroy", "mhdvlct_last_error_string",
     "mhdvlct_courant", "mhdvlct_required_ghost_depth", "mhdvlct_block_step",
+    "mhdvlct_block_step_noalloc",
     "mhdvlct_block_timestep", "mhdvlct_fill_ghosts_periodic",
     "mhdvlct_batch_create", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
@@ -104,6 +105,7 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_courant.argtypes = [vp]
     L.mhdvlct_courant.restype = dp
     L.mhdvlct_block_step.argtypes = [vp, P(MhdBlockView), dp, vp]
+    L.mhdvlct_block_step_noalloc.argtypes = [vp, P(MhdBlockView), dp, vp]
     L.mhdvlct_block_timestep.argtypes = [vp, P(MhdBlockView), P(dp), vp]
     L.mhdvlct_fill_ghosts_periodic.argtypes = [vp, P(MhdBlockView), vp]
     L.mhdvlct_batch_create.argtypes = [vp, P(ip), P(dp), ip, ip, ip, P(vp)]

@@ -122,6 +122,25 @@ int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b, double dt,
 int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
                            double* dt_out, void* stream);
 
+/* No counterpart in the reference (the reference's compute allocates its
+ * scratch through EnzoVlctScratchSpace on the host heap).  Same operation and
+ * results as mhdvlct_block_step, but allocates no device memory: its scratch
+ * is one file-scope __device__ array of 8 MiB (8388608 bytes) per device,
+ * whose address is taken with cudaGetSymbolAddress on the first call on each
+ * device and cached.  Make that first call on a device outside stream
+ * capture.  A block whose scratch (all cell fields and two sets of face
+ * fields at the ghosted extents, plus descriptors) exceeds 8 MiB, or whose
+ * stage needs more than 512 tiles, is rejected with MHD_ERR_INVALID and a
+ * message naming the bytes needed (an FP64 block of 32^3 cells with 3 ghost
+ * zones needs about 6.7 MB).  Nothing in the array has to start at zero:
+ * every call rewrites the dt slot, the stage descriptors and the tile list,
+ * and each intermediate value a stage reads was written earlier in the same
+ * call.  All calls on one device share the array: two calls that overlap in
+ * time (different streams, threads or handles) race on it; order them on one
+ * stream or synchronise between them. */
+int mhdvlct_block_step_noalloc(mhdvlct_handle* h, const MhdBlockView* b,
+                               double dt, void* stream);
+
 /* Same-level periodic ghost refresh of a block onto itself (the effect of
  * Cello's refresh for a single periodic root block,
  * src/Cello/control_refresh.cpp:243-360). */
