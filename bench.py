@@ -55,8 +55,17 @@ def _args():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
-    ap.add_argument("--cpu-sample-blocks", type=int, default=256)
+    ap.add_argument("--cpu-sample-blocks", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mode", default="main",
+                    choices=["main", "amr", "serve", "precision"],
+                    help="main: the contract line; amr / serve / precision: the "
+                         "mixed-size block set, the serving stream, the FP32-vs-FP64 "
+                         "study (one JSON line each)")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--precision-n", type=int, default=512)
+    ap.add_argument("--precision-cycles", type=int, default=50)
     ap.add_argument("--tile", type=str, default="",
                     help="force the stage tile, e.g. 24x12 (skips the autotuner)")
     return ap.parse_args()
@@ -71,17 +80,19 @@ def _dist():
 
 # ------------------------------------------------------------- CPU baseline
 def _cpu_block_cycle(args):
-    """One cycle (timestep, periodic refresh, step) of one block on the CPU
-    oracle; returns active zones updated."""
-    seed, n = args
+    """One cycle (timestep, periodic ghost fill, step) of one block of the
+    workload on the CPU oracle; returns (active zones, compute seconds)."""
+    path, n, w = args
     sys.path.insert(0, ROOT)
     sys.path.insert(0, PKG)
+    import numpy as np
     from oracle import oracle as O
     from mhdvlct import ic
-    s, w = ic.smooth_block(n, GHOST, seed=seed, amp_v=0.8)
+    s = np.load(path)
     b = O.Block(n, GHOST, w)
-    for k, v in s.items():
-        b.f[ic.ORACLE_NAME[k]][...] = v
+    for k in s.files:
+        if k in ic.ORACLE_NAME and ic.ORACLE_NAME[k] in b.f:
+            b.f[ic.ORACLE_NAME[k]][...] = s[k]
     prm = O.params(riemann=O.HLLD, recon=O.PLM, courant=COURANT)
     t = time.perf_counter()
     dt = O.timestep(prm, b)
@@ -90,48 +101,71 @@ def _cpu_block_cycle(args):
     return n ** 3, time.perf_counter() - t
 
 
-def cpu_baseline(nblocks, n, steps=1):
-    """Time the CPU oracle (a port of the reference's CPU path) on `nblocks`
-    blocks of n^3 with every host core; returns (zone-updates/s, cores,
-    seconds)."""
+def cpu_sample(blocks, widths, nblocks, tmpdir):
+    """Write the first `nblocks` blocks of the workload (FP64) to `tmpdir` for
+    the CPU workers; returns the work list."""
+    import numpy as np
+    n = blocks[0]["density"].shape[0] - 2 * GHOST
+    work = []
+    for i in range(min(nblocks, len(blocks))):
+        path = os.path.join(tmpdir, f"block{i}.npz")
+        np.savez(path, **{k: np.asarray(v, dtype=np.float64) for k, v in blocks[i].items()
+                          if k != "pressure"})
+        work.append((path, n, tuple(widths)))
+    return work
+
+
+def cpu_baseline(work, steps=1):
+    """Time the CPU oracle (a port of the reference's CPU path) over the
+    sampled blocks with every host core, one block per process; returns
+    (zone-updates/s, cores, wall seconds of the last step)."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    work = [(1000 + i, n) for i in range(nblocks)]
+    vals = []
+    el = 0.0
     with ctx.Pool(cores) as pool:
         pool.map(_cpu_block_cycle, work[:cores])  # warm the workers
-        t0 = time.perf_counter()
-        zones = 0
         for _ in range(steps):
+            t0 = time.perf_counter()
             res = pool.map(_cpu_block_cycle, work)
-            zones += sum(r[0] for r in res)
-        el = time.perf_counter() - t0
-    return zones / el, cores, el
+            el = time.perf_counter() - t0
+            vals.append(sum(r[0] for r in res) / el)
+    return vals, cores, el
 
 
 def run_reference(a, rank, world):
+    """The reference arm: the CPU oracle (the reference's VL+CT restated in
+    C++, compiled for the host) over the turbulent box's blocks on every host
+    core, `warmup` untimed then `steps` timed samples of one cycle each."""
     if rank != 0:
         return
+    import numpy as np
+    from mhdvlct import ic
     n = a.n // a.nb
-    sample = max(1, a.cpu_sample_blocks)
-    vals = []
-    # warm-up steps are untimed samples too
-    for i in range(a.warmup + a.steps):
-        v, cores, el = cpu_baseline(sample, n)
-        if i >= a.warmup:
-            vals.append(v)
+    blocks, widths = ic.turbulent_box(N=a.n, nb=a.nb, g=GHOST, seed=1, mach=2.0,
+                                      dtype=np.float64)
+    sample = max(1, min(a.cpu_sample_blocks, len(blocks)))
+    with tempfile.TemporaryDirectory() as td:
+        work = cpu_sample(blocks, widths, sample, td)
+        del blocks
+        vals, cores, el = cpu_baseline(work, steps=a.warmup + a.steps)
+    vals = vals[a.warmup:]
     value = statistics.median(vals)
+    desc = (f"{sample} of the {a.nb ** 3} blocks of {n}^3 (+{GHOST} ghosts), one cycle "
+            f"(timestep, ghost fill, VL+CT step) per sample step, CPU oracle restating "
+            f"the reference's C++, one block per process, {el:.1f} s wall per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "zone-updates/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"turbulent box {a.n}^3 in {a.nb ** 3} blocks of {n}^3, HLLD+PLM",
-                   "sample": f"{sample} blocks of {n}^3 (+{GHOST} ghosts), one cycle per step"},
+        "config": {"workload": f"turbulent box {a.n}^3 in {a.nb ** 3} blocks of {n}^3 "
+                               f"(+{GHOST} ghosts), HLLD+PLM, gamma 5/3, CFL {COURANT}",
+                   "sample": desc},
         "cpu_baseline": {"value": value, "unit": "zone-updates/s", "cores": cores,
-                         "kind": "port",
-                         "sample": f"{sample} blocks of {n}^3, 1 cycle, CPU oracle restating the reference, one block per process"},
+                         "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": "zone-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -216,14 +250,15 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic(kernel_key):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/ncu_traffic.json), scaled to this workload."""
+def _traffic(kernel_key, zones):
+    """DRAM bytes per launch of the dominant kernel: the ncu-measured bytes
+    per active zone of that kernel (profiles/ncu_traffic.json, captured on a
+    smaller box of the same 32^3 blocks) times this launch's zones."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
             t = json.load(f)
-        return t.get(kernel_key)
-    except (OSError, ValueError):
+        return t["bytes_per_zone"][kernel_key] * zones
+    except (OSError, ValueError, KeyError):
         return None
 
 
@@ -242,35 +277,302 @@ def aggregate(world: int, zones_per_rank: int, steps: int, ms_local: float):
 
 
 def make_batch(meth, blocks, widths, dtype, nb):
+    """Batch of nb^3 equal blocks of a periodic brick."""
+    from mhdvlct import ic
+    n_blk = len(blocks)
+    n = blocks[0]["density"].shape[0] - 2 * GHOST
+    return make_batch_general(meth, blocks, [(n, n, n)] * n_blk,
+                              [tuple(widths)] * n_blk, dtype, ic.brick_neighbors(nb))
+
+
+FIELD_KEYS = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
+              "internal_energy", "bfield_x", "bfield_y", "bfield_z", "bfieldi_x",
+              "bfieldi_y", "bfieldi_z")
+
+
+def view_pointers(v):
+    return {"density": v.density, "velocity_x": v.velocity[0],
+            "velocity_y": v.velocity[1], "velocity_z": v.velocity[2],
+            "total_energy": v.total_energy, "internal_energy": v.internal_energy,
+            "bfield_x": v.bfield[0], "bfield_y": v.bfield[1], "bfield_z": v.bfield[2],
+            "bfieldi_x": v.bfieldi[0], "bfieldi_y": v.bfieldi[1],
+            "bfieldi_z": v.bfieldi[2]}
+
+
+def make_batch_general(meth, blocks, dims, widths, dtype, nbr):
+    """Batch of arbitrary blocks: dims/widths per block, nbr the 27-neighbour
+    table (nblocks x 27); blocks' host arrays are copied into the pool."""
     import numpy as np
     from mhdvlct import capi
     n_blk = len(blocks)
-    n = blocks[0]["density"].shape[0] - 2 * GHOST
-    dims = (ctypes.c_int * (3 * n_blk))(*([n] * 3 * n_blk))
-    ws = (ctypes.c_double * (3 * n_blk))(*(list(widths) * n_blk))
+    cd = (ctypes.c_int * (3 * n_blk))(*[int(x) for d in dims for x in d])
+    ws = (ctypes.c_double * (3 * n_blk))(*[float(x) for w in widths for x in w])
     h = ctypes.c_void_p()
     L = capi.lib()
-    capi.check(L.mhdvlct_batch_create(meth.handle, dims, ws, n_blk, GHOST, dtype,
+    capi.check(L.mhdvlct_batch_create(meth.handle, cd, ws, n_blk, GHOST, dtype,
                                       ctypes.byref(h)), meth.handle, "batch_create")
-    from mhdvlct import ic
-    nbr = ic.brick_neighbors(nb)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
     capi.check(L.mhdvlct_batch_set_neighbors(
-        h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())), meth.handle, "nbr")
+        h, nbr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), meth.handle, "nbr")
     rt = _cudart()
     npdt = np.float64 if dtype == capi.MHD_DTYPE_F64 else np.float32
     for i, blk in enumerate(blocks):
         v = capi.MhdBlockView()
         capi.check(L.mhdvlct_batch_block_view(h, i, ctypes.byref(v)))
-        ptrs = {"density": v.density, "velocity_x": v.velocity[0],
-                "velocity_y": v.velocity[1], "velocity_z": v.velocity[2],
-                "total_energy": v.total_energy, "bfield_x": v.bfield[0],
-                "bfield_y": v.bfield[1], "bfield_z": v.bfield[2],
-                "bfieldi_x": v.bfieldi[0], "bfieldi_y": v.bfieldi[1],
-                "bfieldi_z": v.bfieldi[2]}
-        for k, p in ptrs.items():
+        for k, p in view_pointers(v).items():
+            if not p or k not in blk:
+                continue
             a = np.ascontiguousarray(blk[k], dtype=npdt)
             assert rt.cudaMemcpy(p, a.ctypes.data, a.nbytes, 1) == 0
     return h
+
+
+def run_serve(seed=4, nreq=24, rate_hz=30.0, cycles=20, budget_gib=6.0,
+              max_active=32):
+    """Serving stream (Poisson arrivals of independent solves): grids on
+    {32,64,96,128}^3, solver on {hlle, hllc (hydro), hlld}, reconstruction on
+    {nn, plm}, FP32, `cycles` cycles each, the turbulent-box recipe at rms Mach
+    uniform in [0.5, 4] with a per-request seed.  Initial states are made
+    before the clock starts; latency is completion minus arrival."""
+    import numpy as np
+    from mhdvlct import serve as S
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(nreq):
+        n = int(rng.choice([32, 64, 96, 128]))
+        solver = str(rng.choice(["hlle", "hllc", "hlld"]))
+        recon = str(rng.choice(["nn", "plm"]))
+        mach = float(rng.uniform(0.5, 4.0))
+        state, box = S.request_state(n, seed * 100003 + i, mach, solver != "hllc")
+        specs.append((n, solver, recon, state, box))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, nreq))
+    srv = S.Server(int(budget_gib * 2 ** 30), max_active=max_active, courant=COURANT)
+    # warm every (solver, reconstruction) kernel once, untimed
+    warm = []
+    for solver in ("hlle", "hllc", "hlld"):
+        for recon in ("nn", "plm"):
+            st, bx = S.request_state(16, 7, 1.0, solver != "hllc")
+            warm.append(srv.submit(st, 16, 2, solver, recon, bx))
+    srv.drain(warm)
+    tickets = [None] * nreq
+    t0 = time.perf_counter()
+    nxt = 0
+    while True:
+        now = time.perf_counter() - t0
+        while nxt < nreq and arrivals[nxt] <= now:
+            n, solver, recon, state, box = specs[nxt]
+            tickets[nxt] = srv.submit(state, n, cycles, solver, recon, box)
+            nxt += 1
+        srv.pump(1)
+        live = [t for t in tickets[:nxt] if srv.poll(t) in (S.QUEUED, S.RUNNING)]
+        if nxt == nreq and not live:
+            break
+        if not live and nxt < nreq:
+            time.sleep(max(0.0, min(0.002, arrivals[nxt] - (time.perf_counter() - t0))))
+    lat, first, last, failed = [], None, None, 0
+    for t in tickets:
+        if srv.poll(t) != S.DONE:
+            failed += 1
+            continue
+        ts, ta, td = srv.timing(t)
+        lat.append(td - ts)
+        first = ts if first is None else min(first, ts)
+        last = td if last is None else max(last, td)
+    zu = sum(sp[0] ** 3 * cycles for sp in specs)
+    srv.close()
+    lat_ms = np.array(lat) * 1e3
+    return {"requests": nreq, "failed": failed, "cycles_per_request": cycles,
+            "arrival_rate_hz": rate_hz, "hbm_budget_gib": budget_gib,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat) else None,
+            "zone_updates_per_s": zu / (last - first) if lat else None,
+            "grids": [32, 64, 96, 128], "dtype": "f32"}
+
+
+def amr_blocks(seed=3, counts=((16, 1200), (32, 600), (64, 200))):
+    """The mixed-size block set: Sedov blasts (E = 1 in a Gaussian of 2
+    cells at a seeded off-centre point, rho = 1, p = 1e-5,
+    B = (0.05, 0.05, 0.05)), sizes shuffled with the seed; each block's
+    ghost zones come from seeded same-size neighbours."""
+    import numpy as np
+    from mhdvlct import ic
+    rng = np.random.default_rng(seed)
+    sizes = np.concatenate([np.full(c, n) for n, c in counts])
+    rng.shuffle(sizes)
+    blocks, dims, widths = [], [], []
+    for i, n in enumerate(sizes):
+        blk, w = ic.sedov_block(int(n), GHOST, seed=seed * 7919 + i, width=1.0,
+                                dtype=np.float32)
+        blk.pop("pressure", None)
+        blocks.append(blk)
+        dims.append((int(n),) * 3)
+        widths.append(w)
+    by_size = {n: np.flatnonzero(sizes == n) for n, _ in counts}
+    nbr = np.empty((len(sizes), 27), dtype=np.int32)
+    for i, n in enumerate(sizes):
+        pool = by_size[n]
+        nbr[i] = rng.choice(pool, size=27)
+        nbr[i, 13] = i
+    return blocks, dims, widths, nbr
+
+
+def run_amr(a):
+    """Mixed-size AMR block set, FP32, per-block dt, one persistent launch per
+    stage over all blocks, tiles from the autotuner."""
+    import numpy as np
+    import torch
+    from mhdvlct import block as B, capi
+    L = capi.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    blocks, dims, widths, nbr = amr_blocks()
+    zones = int(sum(d[0] * d[1] * d[2] for d in dims))
+    meth = B.EnzoMethodMHDVlct(riemann_solver="hlld", reconstruct_method="plm",
+                               courant=COURANT)
+    h = make_batch_general(meth, blocks, dims, widths, capi.MHD_DTYPE_F32, nbr)
+    del blocks
+    tune = None
+    if not a.no_tune:
+        buf = ctypes.create_string_buffer(8192)
+        capi.check(L.mhdvlct_batch_autotune(h, 2, buf, 8192, sp), meth.handle, "autotune")
+        tune = json.loads(buf.value.decode() or "{}")
+    capi.check(L.mhdvlct_batch_run(h, a.warmup, 1, None, sp), meth.handle, "warmup")
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    capi.check(L.mhdvlct_batch_run(h, a.steps, 1, None, sp), meth.handle, "run")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = (ctypes.c_float * 5)()
+    capi.check(L.mhdvlct_batch_profile(h, a.steps, 1, prof, sp), meth.handle, "profile")
+    diag = (ctypes.c_double * 8)()
+    capi.check(L.mhdvlct_batch_diagnostics(h, diag, sp), meth.handle, "diag")
+    L.mhdvlct_batch_destroy(h)
+    return {"mode": "amr", "metric": "zone-updates/s (mixed-size AMR block set)",
+            "value": zones * a.steps / (ms / 1e3), "unit": "zone-updates/s",
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
+            "dtype": "f32", "data": "synthetic (seeded Sedov blasts)",
+            "config": {"workload": "2000 blocks: 1200 x 16^3, 600 x 32^3, 200 x 64^3 "
+                                   "(+3 ghosts), HLLD+PLM, per-block dt",
+                       "zones_per_step": zones, "tuning": tune},
+            "kernels_ms_per_step": dict(zip(("timestep", "refresh", "stage1_half_dt",
+                                             "stage2_full_dt", "cycle"), list(prof))),
+            "gpu_launches": 6 * a.steps, "clocks": clk,
+            "finite": all(np.isfinite(list(diag)))}
+
+
+class _DevArray:
+    """A device buffer seen by torch through __cuda_array_interface__."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"data": (int(ptr), False), "shape": tuple(shape),
+                                         "typestr": typestr, "version": 3,
+                                         "strides": None}
+
+
+def run_precision(a, cycles=50, N=512, nb=8):
+    """FP32 form (float-float internal-energy recovery, FP64 totals and dt)
+    against the FP64 form on the same initial state: turbulent box at rms
+    Mach 4 with dual energy (eta = 0.001), both advanced with the FP64 form's
+    global dt.  Reports per-field relative L1 over the active zones, drift of
+    the FP64 conserved totals and max |div B|."""
+    import numpy as np
+    import torch
+    from mhdvlct import block as B, capi, ic
+    L = capi.lib()
+    sp = torch.cuda.current_stream().cuda_stream
+    n = N // nb
+    nblk = nb ** 3
+    meth = B.EnzoMethodMHDVlct(riemann_solver="hlld", reconstruct_method="plm",
+                               courant=COURANT, dual_energy=True, dual_energy_eta=0.001)
+    w = (1.0 / N,) * 3
+    h64 = make_batch_general(meth, [], [(n, n, n)] * nblk, [w] * nblk,
+                             capi.MHD_DTYPE_F64, ic.brick_neighbors(nb))
+    h32 = make_batch_general(meth, [], [(n, n, n)] * nblk, [w] * nblk,
+                             capi.MHD_DTYPE_F32, ic.brick_neighbors(nb))
+    rt = _cudart()
+
+    def upload(i, blk):
+        for h, npdt in ((h64, np.float64), (h32, np.float32)):
+            v = capi.MhdBlockView()
+            capi.check(L.mhdvlct_batch_block_view(h, i, ctypes.byref(v)))
+            for k, p in view_pointers(v).items():
+                if p and k in blk:
+                    a = np.ascontiguousarray(blk[k], dtype=npdt)
+                    assert rt.cudaMemcpy(p, a.ctypes.data, a.nbytes, 1) == 0
+
+    # the initial state streams block by block into both forms
+    ic.turbulent_box(N=N, nb=nb, g=GHOST, seed=11, mach=4.0, dtype=np.float64,
+                     dual_energy=True, sink=upload)
+    dts = (ctypes.c_double * nblk)()
+    dts32 = (ctypes.c_double * nblk)()
+    m = n + 2 * GHOST
+    act = (slice(GHOST, GHOST + n),) * 3
+    keys = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
+            "internal_energy", "bfield_x", "bfield_y", "bfield_z")
+
+    def l1():
+        num = {k: 0.0 for k in keys}
+        den = {k: 0.0 for k in keys}
+        for i in range(nblk):
+            v64, v32 = capi.MhdBlockView(), capi.MhdBlockView()
+            capi.check(L.mhdvlct_batch_block_view(h64, i, ctypes.byref(v64)))
+            capi.check(L.mhdvlct_batch_block_view(h32, i, ctypes.byref(v32)))
+            p64, p32 = view_pointers(v64), view_pointers(v32)
+            for k in keys:
+                x = torch.as_tensor(_DevArray(p64[k], (m, m, m), "<f8"), device="cuda")[act]
+                y = torch.as_tensor(_DevArray(p32[k], (m, m, m), "<f4"), device="cuda")[act]
+                num[k] += float((y.double() - x).abs().sum())
+                den[k] += float(x.abs().sum())
+        return {k: num[k] / den[k] if den[k] > 0 else num[k] for k in keys}
+
+    def diag(h):
+        d = (ctypes.c_double * 8)()
+        capi.check(L.mhdvlct_batch_diagnostics(h, d, sp))
+        return list(d)
+
+    d0 = {"fp64": diag(h64), "fp32": diag(h32)}
+    report = {"l1": {}, "drift": {}, "max_divb": {}, "max_rel_dt_diff": 0.0}
+    t0 = time.perf_counter()
+    for c in range(1, cycles + 1):
+        capi.check(L.mhdvlct_batch_timestep(h64, dts, sp))
+        capi.check(L.mhdvlct_batch_timestep(h32, dts32, sp))
+        dtm = min(dts)
+        report["max_rel_dt_diff"] = max(report["max_rel_dt_diff"],
+                                        abs(min(dts32) - dtm) / dtm)
+        glob = (ctypes.c_double * nblk)(*([dtm] * nblk))
+        for h in (h64, h32):
+            capi.check(L.mhdvlct_batch_refresh(h, sp))
+            capi.check(L.mhdvlct_batch_step(h, glob, sp))
+        if c in (1, 10, cycles):
+            report["l1"][str(c)] = l1()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    for tag, h in (("fp64", h64), ("fp32", h32)):
+        d = diag(h)
+        ref = d0[tag]
+        report["drift"][tag] = {
+            "mass": (d[0] - ref[0]) / abs(ref[0]),
+            "energy": (d[4] - ref[4]) / abs(ref[4]),
+            "momentum": [(d[1 + k] - ref[1 + k]) / max(abs(ref[1 + k]), 1e-300)
+                         for k in range(3)],
+            "momentum_abs": [d[1 + k] - ref[1 + k] for k in range(3)],
+        }
+        report["max_divb"][tag] = d[6]
+        report["max_divb_normalised"] = report.get("max_divb_normalised", {})
+        report["max_divb_normalised"][tag] = d[6] * (1.0 / N) / d[7] if d[7] > 0 else None
+    L.mhdvlct_batch_destroy(h64)
+    L.mhdvlct_batch_destroy(h32)
+    report.update({"mode": "precision", "cycles": cycles, "wall_s": wall,
+                   "config": {"workload": f"turbulent box {N}^3 in {nb ** 3} blocks of "
+                                          f"{n}^3 (+{GHOST} ghosts), rms Mach 4, HLLD+PLM, "
+                                          f"dual energy eta 0.001, FP64 global dt"}})
+    return report
 
 
 def main():
@@ -295,6 +597,20 @@ def main():
     import torch
     from mhdvlct import block as B, capi, ic
     torch.cuda.set_device(local)
+    if a.mode != "main":
+        if rank == 0:
+            if a.mode == "amr":
+                out = run_amr(a)
+            elif a.mode == "serve":
+                out = {"mode": "serve", **run_serve(nreq=a.serve_requests)}
+            else:
+                out = run_precision(a, cycles=a.precision_cycles, N=a.precision_n)
+            print(json.dumps(out), flush=True)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     L = capi.lib()
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -354,7 +670,7 @@ def main():
     else:
         dom, dom_ms, dom_bytes = "stage1_half_dt", k_s1, bytes_s1
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    traffic = _traffic(dom)
+    traffic = _traffic(dom, zones)
 
     # ------------------------------------------------------ e2e (host data)
     e2e = None
@@ -427,15 +743,23 @@ def main():
         fp64["fp32_batched_over_plain_fp64"] = value / world / fp64["plain_fp64_zone_updates_per_s"]
         L.mhdvlct_batch_destroy(h64)
 
+    # -------------------------------------------------------- serving stream
+    serving = None
+    if rank == 0 and not a.no_serve:
+        serving = run_serve(nreq=a.serve_requests)
+
     # ----------------------------------------------------------- CPU baseline
     cpu = None
     if rank == 0 and not a.no_cpu:
-        sample = max(1, a.cpu_sample_blocks)
-        cv, cores, el = cpu_baseline(sample, n)
-        cpu = {"value": cv, "unit": "zone-updates/s", "cores": cores, "kind": "port",
-               "sample": f"{sample} blocks of {n}^3 (+{GHOST} ghosts), one cycle each, "
-                         f"CPU oracle restating the reference, one block per process, "
-                         f"{el:.1f} s wall"}
+        sample = max(1, min(a.cpu_sample_blocks, len(blocks)))
+        with tempfile.TemporaryDirectory() as td:
+            work = cpu_sample(blocks, widths, sample, td)
+            vals, cores, el = cpu_baseline(work, steps=2)
+        cpu = {"value": vals[-1], "unit": "zone-updates/s", "cores": cores, "kind": "port",
+               "sample": f"{sample} of the {a.nb ** 3} blocks of {n}^3 (+{GHOST} ghosts), "
+                         f"one cycle each (timestep, ghost fill, step), CPU oracle "
+                         f"restating the reference's C++, one block per process, "
+                         f"{el:.1f} s wall (second of two passes)"}
 
     if rank == 0:
         line = {
@@ -462,6 +786,7 @@ def main():
             "clocks": clk,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "serving": serving,
         }
         line.update(fp64)
         print(json.dumps(line), flush=True)

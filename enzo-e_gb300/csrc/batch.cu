@@ -66,6 +66,8 @@ struct mhdvlct_batch {
   double* d_dtmin = nullptr;
   double* d_time = nullptr;
   void* d_smax = nullptr;
+  double* d_diag = nullptr;   // diagnostics: partial rows then the 8 totals
+  int diag_rows = 0;
   int grid = 0;               // persistent grid size (0 = fill the GPU)
   int threads = 256;          // CTA size of the stage launches
   std::map<std::vector<int>, TileChoice> tune;  // per block-size class
@@ -377,6 +379,7 @@ extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
   cudaFree(b->d_dtmin);
   cudaFree(b->d_time);
   cudaFree(b->d_smax);
+  cudaFree(b->d_diag);
   cudaFree(b->pool);
   delete b;
   return MHD_OK;
@@ -683,6 +686,39 @@ extern "C" int mhdvlct_batch_profile(mhdvlct_batch* b, int reps, int dt_mode,
   cudaStream_t st = (cudaStream_t)stream;
   return b->dtype == MHD_DTYPE_F64 ? profile_t<double>(b, reps, dt_mode, ms_out, st)
                                    : profile_t<float>(b, reps, dt_mode, ms_out, st);
+}
+
+extern "C" int mhdvlct_batch_diagnostics(mhdvlct_batch* b, double* out, void* stream) {
+  if (!b || !out) return MHD_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t cells = 0;
+  for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
+  const size_t per = std::max<size_t>(1, cells / b->nblocks);
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 4096, 64));
+  const int rows = b->nblocks * cpb;
+  if (!b->d_diag || b->diag_rows < rows) {
+    cudaStreamSynchronize(st);
+    cudaFree(b->d_diag);
+    b->d_diag = nullptr;
+    if (cudaMalloc((void**)&b->d_diag, ((size_t)rows + 1) * NDIAG * sizeof(double)) !=
+        cudaSuccess) {
+      b->d_diag = nullptr;
+      return bfail(b, MHD_ERR_NOMEM, "diagnostics scratch");
+    }
+    b->diag_rows = rows;
+  }
+  double* tot = b->d_diag + (size_t)b->diag_rows * NDIAG;
+  cudaError_t e =
+      b->dtype == MHD_DTYPE_F64
+          ? launch_diag<double>((const AuxBlock<double>*)b->d_aux[b->parity], b->nblocks,
+                                b->g, cpb, b->h->mhd != 0, b->h->de != 0, b->d_diag, tot, st)
+          : launch_diag<float>((const AuxBlock<float>*)b->d_aux[b->parity], b->nblocks,
+                               b->g, cpb, b->h->mhd != 0, b->h->de != 0, b->d_diag, tot, st);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, std::string("diagnostics: ") + cudaGetErrorString(e));
+  e = cudaMemcpyAsync(out, tot, NDIAG * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, std::string("diagnostics: ") + cudaGetErrorString(e));
+  return MHD_OK;
 }
 
 extern "C" int mhdvlct_batch_autotune(mhdvlct_batch* b, int reps, char* json_out,

@@ -269,3 +269,120 @@ __global__ void copy_faces_kernel(int m0, int m1, int m2, int lo_t, int S1,
 static __global__ void set_scalar_kernel(double* p, double v) { *p = v; }
 
 }  // namespace vlct
+
+namespace vlct {
+
+// ---------------------------------------------------------------------------
+// Conserved totals and constraint diagnostics over the active zones of every
+// block, accumulated in FP64 whatever the storage precision:
+//   [0] mass  sum rho dV            [1..3] momentum  sum rho v_d dV
+//   [4] energy sum rho e_tot dV     [5] sum rho e_int dV (dual energy)
+//   [6] max |div B| (face B, per cell, 1/length units)
+//   [7] max |B_cell|
+// Each CTA reduces its share in a fixed order and writes one partial row; the
+// finishing kernel adds the rows in a fixed order, so the totals are
+// bit-reproducible run to run.
+// ---------------------------------------------------------------------------
+constexpr int NDIAG = 8;
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// max that keeps a NaN (a NaN in a diagnostic must not be hidden)
+__device__ __forceinline__ double nan_max(double a, double b) {
+  return (b > a || b != b) ? b : a;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+diag_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks, int g, int cpb,
+            int mhd, int de, double* __restrict__ partial) {
+  __shared__ double red[NDIAG][8];
+  const int b = blockIdx.x / cpb;
+  const int chunk = blockIdx.x - b * cpb;
+  if (b >= nblocks) return;
+  const AuxBlock<R>& B = blocks[b];
+  const int m0 = B.m[0], m1 = B.m[1];
+  const int n0 = B.m[0] - 2 * g, n1 = B.m[1] - 2 * g, n2 = B.m[2] - 2 * g;
+  const size_t nact = (size_t)n0 * n1 * n2;
+  double acc[NDIAG] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (size_t idx = (size_t)chunk * blockDim.x + threadIdx.x; idx < nact;
+       idx += (size_t)cpb * blockDim.x) {
+    const size_t row = idx / n0;
+    const int x = (int)(idx - row * n0) + g;
+    const int y = (int)(row % n1) + g;
+    const int z = (int)(row / n1) + g;
+    const size_t c = ((size_t)z * m1 + y) * m0 + x;
+    const double rho = (double)B.f.c[F_RHO][c];
+    acc[0] += rho;
+    acc[1] += rho * (double)B.f.c[F_VX][c];
+    acc[2] += rho * (double)B.f.c[F_VY][c];
+    acc[3] += rho * (double)B.f.c[F_VZ][c];
+    acc[4] += rho * (double)B.f.c[F_ETOT][c];
+    if (de) acc[5] += rho * (double)B.f.c[F_EINT][c];
+    if (mhd) {
+      const R* fx = B.f.f[0];
+      const R* fy = B.f.f[1];
+      const R* fz = B.f.f[2];
+      const size_t ix = ((size_t)z * m1 + y) * (m0 + 1) + x;
+      const size_t iy = ((size_t)z * (m1 + 1) + y) * m0 + x;
+      const size_t iz = c;
+      const size_t sz = (size_t)m0 * m1;
+      const double div = ((double)fx[ix + 1] - (double)fx[ix]) / B.cw[0] +
+                         ((double)fy[iy + m0] - (double)fy[iy]) / B.cw[1] +
+                         ((double)fz[iz + sz] - (double)fz[iz]) / B.cw[2];
+      acc[6] = nan_max(acc[6], fabs(div));
+      const double bx = B.f.c[F_BX][c], by = B.f.c[F_BY][c], bz = B.f.c[F_BZ][c];
+      acc[7] = nan_max(acc[7], sqrt(bx * bx + by * by + bz * bz));
+    }
+  }
+  const double dV = B.cw[0] * B.cw[1] * B.cw[2];
+  for (int k = 0; k < 6; k++) acc[k] *= dV;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NDIAG; k++) {
+    const double v = k < 6 ? warp_sum(acc[k]) : warp_max(acc[k]);
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NDIAG) {
+    const int k = threadIdx.x;
+    double v = red[k][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+      v = k < 6 ? v + red[k][w] : nan_max(v, red[k][w]);
+    partial[(size_t)blockIdx.x * NDIAG + k] = v;
+  }
+}
+
+static __global__ void __launch_bounds__(256)
+diag_finish_kernel(const double* __restrict__ partial, int nrows, double* __restrict__ out) {
+  __shared__ double red[NDIAG][8];
+  double acc[NDIAG] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int r = threadIdx.x; r < nrows; r += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NDIAG; k++) {
+      const double v = partial[(size_t)r * NDIAG + k];
+      acc[k] = k < 6 ? acc[k] + v : nan_max(acc[k], v);
+    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NDIAG; k++) {
+    const double v = k < 6 ? warp_sum(acc[k]) : warp_max(acc[k]);
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NDIAG) {
+    const int k = threadIdx.x;
+    double v = red[k][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+      v = k < 6 ? v + red[k][w] : nan_max(v, red[k][w]);
+    out[k] = v;
+  }
+}
+
+}  // namespace vlct

@@ -135,4 +135,16 @@ cudaError_t launch_copy_faces<VLCT_REAL>(int m0, int m1, int m2, int S1,
   return cudaGetLastError();
 }
 
+template <>
+cudaError_t launch_diag<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, int nb, int g, int cpb,
+                                   bool mhd, bool de, double* partial, double* out,
+                                   cudaStream_t st) {
+  diag_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nb, g, cpb, mhd ? 1 : 0, de ? 1 : 0,
+                                                   partial);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  diag_finish_kernel<<<1, 256, 0, st>>>(partial, nb * cpb, out);
+  return cudaGetLastError();
+}
+
 }  // namespace vlct

@@ -42,6 +42,13 @@ cudaError_t launch_copy_faces(int m0, int m1, int m2, int S1, const R* fx,
                               const R* fy, const R* fz, R* ox, R* oy, R* oz,
                               cudaStream_t st);
 
+// FP64 conserved totals / div B of every block's active zones into out[8];
+// partial: nb * cpb * 8 doubles of scratch.
+template <class R>
+cudaError_t launch_diag(const AuxBlock<R>* d_blocks, int nblocks, int g, int cpb,
+                        bool mhd, bool de, double* partial, double* out,
+                        cudaStream_t st);
+
 cudaError_t launch_set_scalar(double* p, double v, cudaStream_t st);
 
 }  // namespace vlct

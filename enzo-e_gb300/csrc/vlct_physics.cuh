@@ -60,7 +60,7 @@ template <class R>
 __device__ __forceinline__ R eint_flux(R g, R dl, R pl, R dr, R pr, R fd) {
   const R el = specific_eint(g, dl, pl);
   const R er = specific_eint(g, dr, pr);
-  const R up = R(fd > R(0)) * el + R(fd <= R(0)) * er;
+  const R up = ((fd > R(0)) ? R(1) : R(0)) * el + ((fd <= R(0)) ? R(1) : R(0)) * er;
   return up * fd;
 }
 
@@ -71,8 +71,10 @@ __device__ __forceinline__ R limiter_enzo_rk(R vm1, R v, R vp1, R theta) {
   R dv_c = R(0.5) * (vp1 - vm1);
   R dv_l = (v - vm1) * theta;
   R dv_r = (vp1 - v) * theta;
-  R sl = R((R(0.0) < dv_l) - (dv_l < R(0.0)));
-  R sr = R((R(0.0) < dv_r) - (dv_r < R(0.0)));
+  // sign(dv) in {-1, 0, 1} (the reference's (0 < x) - (x < 0)) as selects,
+  // with no integer-to-float conversion
+  R sl = (R(0.0) < dv_l) ? R(1.0) : ((dv_l < R(0.0)) ? R(-1.0) : R(0.0));
+  R sr = (R(0.0) < dv_r) ? R(1.0) : ((dv_r < R(0.0)) ? R(-1.0) : R(0.0));
   return (R(0.5) * (sl + sr)) * min3(fabs(dv_l), fabs(dv_r), fabs(dv_c));
 }
 // PLM_AthenaLimiter (EnzoReconstructorPLM.hpp:337-345)

@@ -34,7 +34,8 @@ EXPORTED = (
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
     "mhdvlct_batch_refresh", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
     "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_autotune",
-    "mhdvlct_batch_state_region", "mhdvlct_batch_profile", "mhdserve_create",
+    "mhdvlct_batch_state_region", "mhdvlct_batch_profile",
+    "mhdvlct_batch_diagnostics", "mhdserve_create",
     "mhdserve_destroy", "mhdserve_submit", "mhdserve_pump", "mhdserve_poll",
     "mhdserve_result", "mhdserve_timing", "mhdserve_last_error_string",
 )
@@ -120,6 +121,7 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_batch_autotune.argtypes = [vp, ip, ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mhdvlct_batch_state_region.argtypes = [vp, P(vp), P(ctypes.c_size_t)]
     L.mhdvlct_batch_profile.argtypes = [vp, ip, ip, P(ctypes.c_float), vp]
+    L.mhdvlct_batch_diagnostics.argtypes = [vp, P(dp), vp]
     L.mhdserve_create.argtypes = [P(MhdVlctParams), ctypes.c_size_t, ip, P(vp)]
     L.mhdserve_destroy.argtypes = [vp]
     L.mhdserve_submit.argtypes = [vp, P(MhdServeRequest), P(ip)]

@@ -107,18 +107,21 @@ def _grf(shape, kmin, kmax, slope, rng):
     # P(k) ~ k^slope in 3D shells: per-mode amplitude^2 ~ k^(slope-2)
     amp[sel] = K[sel] ** ((slope - 2.0) / 2.0)
     ph = rng.normal(size=K.shape) + 1j * rng.normal(size=K.shape)
-    f = np.fft.irfftn(amp * ph, s=shape)
+    f = np.fft.irfftn(amp * ph, s=shape, axes=(0, 1, 2))
     f -= f.mean()
     s = f.std()
     return f / s if s > 0 else f
 
 
 def turbulent_box(N=256, nb=8, g=3, seed=0, mach=2.0, sigma_ln=0.5, b0=0.2,
-                  beta=1.0, p_over_rho=0.1, gamma=GAMMA, dtype=np.float64):
+                  beta=1.0, p_over_rho=0.1, gamma=GAMMA, dtype=np.float64,
+                  dual_energy=False, sink=None):
     """The turbulent periodic box: N^3 cells split into nb^3 blocks of
     (N/nb)^3 active cells with g ghost layers (filled periodically).
     Returns (blocks, widths) with blocks[(kz*nb + ky)*nb + kx] a dict of
-    arrays in Cello layout."""
+    arrays in Cello layout (with internal_energy when dual_energy).  With
+    `sink`, each block is passed to sink(index, block) instead of being kept
+    (blocks is then empty)."""
     rng = np.random.default_rng(seed)
     shape = (N, N, N)
     G = _grf(shape, 1, 8, -2.0, rng)
@@ -168,8 +171,13 @@ def turbulent_box(N=256, nb=8, g=3, seed=0, mach=2.0, sigma_ln=0.5, b0=0.2,
                        "total_energy": _energy(r, vx, vy, vz, p[cell], bx, by,
                                                bz, gamma),
                        "pressure": np.zeros_like(r)}
-                blocks.append({k: np.ascontiguousarray(v, dtype=dtype)
-                               for k, v in blk.items()})
+                if dual_energy:
+                    blk["internal_energy"] = p[cell] / ((gamma - 1.0) * r)
+                blk = {k: np.ascontiguousarray(v, dtype=dtype) for k, v in blk.items()}
+                if sink is not None:
+                    sink((kz * nb + ky) * nb + kx, blk)
+                else:
+                    blocks.append(blk)
     return blocks, (dx, dx, dx)
 
 

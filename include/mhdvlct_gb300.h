@@ -192,6 +192,15 @@ int mhdvlct_batch_autotune(mhdvlct_batch* b, int reps, char* json_out,
  * state (cell fields and both face-B buffers), for bulk host transfers. */
 int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,
                                size_t* bytes);
+/* Conserved totals and constraint diagnostics of the current state over the
+ * active zones of every block, accumulated on the device in FP64 (whatever
+ * the storage precision) in a fixed order, so bit-reproducible:
+ * out[0] mass, out[1..3] momentum, out[4] total energy (sum rho e_tot dV),
+ * out[5] sum rho e_int dV (dual energy, else 0), out[6] max |div B| over
+ * cells (from the face-centred B), out[7] max |B| at cell centres.
+ * Synchronises the stream.  (The reference computes such sums in its
+ * analysis scripts; no Method counterpart.) */
+int mhdvlct_batch_diagnostics(mhdvlct_batch* b, double* out, void* stream);
 /* Run `reps` cycles as individual launches with CUDA events between the
  * kernels; ms_out[0..4] = mean ms per cycle of the timestep reduction, the
  * ghost refresh, stage 1 (half dt), stage 2 (full dt) and the whole cycle. */

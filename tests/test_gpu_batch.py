@@ -194,3 +194,51 @@ def test_graph_run_matches_oracle_cycles():
         act = (slice(g, g + 8),) * 3
         for k in KEYS[:8]:
             assert np.array_equal(got[k][act], obs[i].f[ic.ORACLE_NAME[k]][act]), (i, k)
+
+
+def _diag(bt):
+    d = (ctypes.c_double * 8)()
+    capi.check(capi.lib().mhdvlct_batch_diagnostics(bt.h, d, None))
+    return list(d)
+
+
+@pytest.mark.parametrize("dtype", [capi.MHD_DTYPE_F64, capi.MHD_DTYPE_F32])
+def test_diagnostics_totals_and_conservation(dtype):
+    """FP64 totals of the active zones match a numpy FP64 sum of the same
+    stored values, repeat bit for bit, and stay conserved over periodic
+    cycles (mass and momentum to round-off; energy is conserved too since
+    the floors are inactive); div B stays at round-off."""
+    meth = B.EnzoMethodMHDVlct()
+    nb, N = 2, 24
+    blocks, w = ic.turbulent_box(N=N, nb=nb, g=3, seed=21, mach=1.5)
+    bt = Batch(meth, [(12, 12, 12)] * 8, [w] * 8, dtype=dtype)
+    nbr = ic.brick_neighbors(nb)
+    capi.check(capi.lib().mhdvlct_batch_set_neighbors(
+        bt.h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())))
+    for i, s in enumerate(blocks):
+        bt.upload(i, s)
+    d0 = _diag(bt)
+    assert _diag(bt) == d0
+    g, n = 3, 12
+    act = (slice(g, g + n),) * 3
+    dv = w[0] * w[1] * w[2]
+    ref = np.zeros(5)
+    for i in range(8):
+        f = {k: a.astype(np.float64)[act] for k, a in bt.download(i).items()
+             if not k.startswith("bfieldi")}
+        rho = f["density"]
+        ref += [rho.sum() * dv, (rho * f["velocity_x"]).sum() * dv,
+                (rho * f["velocity_y"]).sum() * dv, (rho * f["velocity_z"]).sum() * dv,
+                (rho * f["total_energy"]).sum() * dv]
+    np.testing.assert_allclose(d0[:5], ref, rtol=1e-12, atol=1e-14)
+    capi.check(capi.lib().mhdvlct_batch_run(bt.h, 3, 0, None, None))
+    d1 = _diag(bt)
+    tol = 1e-13 if dtype == capi.MHD_DTYPE_F64 else 2e-6
+    assert abs(d1[0] - d0[0]) <= tol * abs(d0[0])
+    assert abs(d1[4] - d0[4]) <= tol * abs(d0[4])
+    scale = d0[0] * 3.0  # momentum scale: mass x rms speed
+    for k in (1, 2, 3):
+        assert abs(d1[k] - d0[k]) <= tol * scale
+    bmax = d1[7]
+    divb_tol = 1e-12 if dtype == capi.MHD_DTYPE_F64 else 1e-5
+    assert d1[6] * w[0] / bmax <= divb_tol
