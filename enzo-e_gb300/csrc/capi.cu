@@ -317,6 +317,11 @@ extern "C" int mhdvlct_create(const MhdVlctParams* p, mhdvlct_handle** out) {
   if (ts == "vl") h->euler = 0;
   else if (ts == "euler") h->euler = 1;
   else return bad("time_scheme must be \"vl\" or \"euler\"");
+  // EnzoBfieldMethod::EnzoBfieldMethod (toolkit/EnzoBfieldMethod.cpp:15-28):
+  // constrained transport with one partial timestep is an ERROR
+  if (h->euler && h->mhd)
+    return bad("constrained_transport hasn't been tested for num_partial_timesteps != 2 "
+               "(time_scheme \"euler\" needs mhd_choice \"no_bfield\")");
   if (h->params.courant < 0) h->params.courant = h->euler ? 1.0 : 0.3;
   if (!(p->gamma > 1.0)) return bad("gamma should exceed 1.0");
   // EnzoMHDIntegratorStageCommands ctor (EnzoMHDIntegratorStageCommands.cpp:35-40)

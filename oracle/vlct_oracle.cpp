@@ -1008,6 +1008,9 @@ extern "C" int oracle_step(const OracleParams* p, OracleBlock* b, double dt) {
   V3 tface[3] = {sc.temp_face[0].w, sc.temp_face[1].w, sc.temp_face[2].w};
   const double cw[3] = {b->dx, b->dy, b->dz};
 
+  // EnzoBfieldMethod.cpp:23-27: constrained transport requires the two
+  // partial timesteps of the vl scheme (the reference ERRORs otherwise)
+  if (p->euler && c.mhd) return 3;
   const int nstages = p->euler ? 1 : 2;
   int stale = 0;
   for (int st = 0; st < nstages; st++) {

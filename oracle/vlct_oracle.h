@@ -44,7 +44,9 @@ typedef struct {
   double *pressure;                              /* [w] scratch field         */
 } OracleBlock;
 
-/* One full VL+CT step of size dt on one ghosted block, in place. */
+/* One full VL+CT step of size dt on one ghosted block, in place.  Returns 0,
+ * or 3 for the euler scheme with magnetic fields (the reference ERRORs:
+ * EnzoBfieldMethod.cpp:23-27). */
 int oracle_step(const OracleParams* p, OracleBlock* b, double dt);
 
 /* The Method::timestep of the reference: syncs energies (dual energy), writes

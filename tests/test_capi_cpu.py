@@ -54,12 +54,16 @@ def test_removed_parameters_rejected():
     (dict(theta_limiter=2.5), False),
     (dict(reconstruct_method="weno"), False),
     (dict(density_floor=0.0), False),
+    # EnzoBfieldMethod.cpp:23-27: constrained transport needs the vl scheme
+    (dict(mhd_choice="constrained_transport", time_scheme="euler"), False),
+    (dict(mhd_choice="no_bfield", riemann_solver="hllc", time_scheme="euler"), True),
 ])
 def test_create_validation(kw, ok):
     if ok:
         m = B.EnzoMethodMHDVlct(**kw)
         assert m.name() == "mhd_vlct"
-        assert m.required_ghost_depth() == 3
+        # vl: NN (1) + PLM (2); euler: one PLM stage (2)
+        assert m.required_ghost_depth() == (2 if kw.get("time_scheme") == "euler" else 3)
     else:
         with pytest.raises(capi.MhdError):
             B.EnzoMethodMHDVlct(**kw)
@@ -67,5 +71,6 @@ def test_create_validation(kw, ok):
 
 def test_default_courant_follows_time_scheme():
     assert B.EnzoMethodMHDVlct().courant == 0.3
-    assert B.EnzoMethodMHDVlct(time_scheme="euler",
+    assert B.EnzoMethodMHDVlct(time_scheme="euler", mhd_choice="no_bfield",
+                               riemann_solver="hllc",
                                reconstruct_method="nn").courant == 1.0

@@ -24,7 +24,7 @@ CASES = [
     ("hllc", "plm", False, "vl"),
     ("hlld", "plm", True, "vl"),
     ("hllc", "plm", True, "vl"),
-    ("hlld", "nn", False, "euler"),
+    ("hllc", "nn", False, "euler"),
 ]
 
 

@@ -51,7 +51,7 @@ def _same(a, b):
 @pytest.mark.parametrize("solver,recon,de,scheme,n,dtype", [
     ("hlld", "plm", False, "vl", (8, 6, 7), torch.float64),
     ("hllc", "plm", True, "vl", (8, 8, 8), torch.float64),
-    ("hlld", "nn", False, "euler", (6, 7, 8), torch.float64),
+    ("hllc", "nn", False, "euler", (6, 7, 8), torch.float64),
     ("hlld", "plm", False, "vl", (12, 12, 12), torch.float32),
 ])
 def test_noalloc_matches_allocating_step_two_calls(solver, recon, de, scheme, n, dtype):
