@@ -304,7 +304,7 @@ def make_batch_general(meth, blocks, dims, widths, dtype, nbr):
     table (nblocks x 27); blocks' host arrays are copied into the pool."""
     import numpy as np
     from mhdvlct import capi
-    n_blk = len(blocks)
+    n_blk = len(dims)
     cd = (ctypes.c_int * (3 * n_blk))(*[int(x) for d in dims for x in d])
     ws = (ctypes.c_double * (3 * n_blk))(*[float(x) for w in widths for x in w])
     h = ctypes.c_void_p()
@@ -551,6 +551,9 @@ def run_precision(a, cycles=50, N=512, nb=8):
             capi.check(L.mhdvlct_batch_step(h, glob, sp))
         if c in (1, 10, cycles):
             report["l1"][str(c)] = l1()
+            dd = {"fp64": diag(h64), "fp32": diag(h32)}
+            report.setdefault("max_divb_normalised_by_cycle", {})[str(c)] = {
+                k: v[6] * (1.0 / N) / v[7] if v[7] > 0 else None for k, v in dd.items()}
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     for tag, h in (("fp64", h64), ("fp32", h32)):

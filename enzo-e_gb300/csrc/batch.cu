@@ -605,8 +605,21 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
     }
     std::sort(shapes.begin(), shapes.end());
     shapes.erase(std::unique(shapes.begin(), shapes.end()), shapes.end());
+    // one launch serves every class, so its shared memory is sized by the
+    // largest tile extents over all classes: a candidate is kept only if that
+    // combined shape fits
+    int other_tx = 1, other_ty = 1;
+    for (int i = 0; i < b->nblocks; i++) {
+      if (b->dims[3 * i] == cls[0] && b->dims[3 * i + 1] == cls[1] &&
+          b->dims[3 * i + 2] == cls[2])
+        continue;
+      const TileChoice oc = choice_for(b, i);
+      other_tx = std::max(other_tx, oc.tile_x);
+      other_ty = std::max(other_ty, oc.tile_y);
+    }
     for (auto& sh : shapes) {
-      if (stage_smem<R>(b->h->solver, b->h->recon, b->h->de != 0, sh.first, sh.second) >
+      if (stage_smem<R>(b->h->solver, b->h->recon, b->h->de != 0,
+                        std::max(sh.first, other_tx), std::max(sh.second, other_ty)) >
           smem_cap)
         continue;
       for (int zc : {0, 16}) {
@@ -644,6 +657,11 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
         cudaEventRecord(e1, st);
         cudaEventSynchronize(e1);
         cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaErrorInvalidValue || e == cudaErrorInvalidConfiguration) {
+          // a launch shape this GPU refuses (nothing ran): skip the candidate
+          e = cudaSuccess;
+          continue;
+        }
         if (e != cudaSuccess) break;
         float t;
         cudaEventElapsedTime(&t, e0, e1);

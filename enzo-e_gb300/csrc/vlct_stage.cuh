@@ -41,18 +41,6 @@ __device__ __forceinline__ bool inr(int a, int lo, int hi) {
   return a >= lo && a < hi;
 }
 
-// Division by a runtime divisor d < 2^16 of a numerator n < 2^16, by a
-// multiply-high with ceil(2^32 / d) (exact because n * d < 2^32).
-struct FastDiv {
-  unsigned d, m;
-  // ceil(2^32 / d) == floor((2^32 - 1) / d) + 1 for every d > 1
-  __device__ __forceinline__ explicit FastDiv(unsigned dd)
-      : d(dd), m(dd > 1 ? 0xFFFFFFFFu / dd + 1u : 0u) {}
-  __device__ __forceinline__ int div(int n) const {
-    return d > 1 ? (int)__umulhi((unsigned)n, m) : n;
-  }
-};
-
 // Upwind weight of CT from the sign of the density flux
 // (EnzoBfieldMethodCT.cpp:198-213).
 template <class R> __device__ __forceinline__ R upw(R fd) {

@@ -54,4 +54,19 @@ struct StageInfo {
   int threads;      // CTA size (256 or 512); 0 = 256
 };
 
+#ifdef __CUDACC__
+// Division by a runtime divisor d > 0 by a multiply-high with ceil(2^32 / d):
+// exact for every numerator n with n * d < 2^32 (m d = 2^32 + e, 0 < e <= d,
+// so n m / 2^32 = n / d + n e / (d 2^32) and n e < 2^32).
+struct FastDiv {
+  unsigned d, m;
+  // ceil(2^32 / d) == floor((2^32 - 1) / d) + 1 for every d > 1
+  __device__ __forceinline__ explicit FastDiv(unsigned dd)
+      : d(dd), m(dd > 1 ? 0xFFFFFFFFu / dd + 1u : 0u) {}
+  __device__ __forceinline__ int div(int n) const {
+    return d > 1 ? (int)__umulhi((unsigned)n, m) : n;
+  }
+};
+#endif
+
 }  // namespace vlct
