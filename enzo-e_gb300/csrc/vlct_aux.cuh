@@ -193,44 +193,25 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
     const int cy = iz * wy * e[0];
     const int cx = iz * iy * wx;
     const int total = cz + cy + cx;
-    // the shell index decodes with multiply-high divisions, exact while
-    // total * divisor < 2^32 (always for blocks up to ~200^3); larger blocks
-    // take the hardware integer division
-    const unsigned dmax = (unsigned)max(max(e[0], e[1]), max(max(wx, wy), iy));
-    const bool fast = (unsigned long long)total * dmax < (1ull << 32);
-    const FastDiv f0(e[0]), f1(e[1]), fwy(wy), fwx(wx), fiy(iy);
-    auto dv = [&](int v, const FastDiv& f) -> int { return fast ? f.div(v) : v / (int)f.d; };
     for (int q = chunk * blockDim.x + threadIdx.x; q < total;
          q += chunks_per_block * blockDim.x) {
       int x, y, z;
       if (q < cz) {
         int r = q;
-        int t = dv(r, f0);
-        x = r - t * e[0];
-        r = t;
-        t = dv(r, f1);
-        y = r - t * e[1];
-        r = t;
+        x = r % e[0]; r /= e[0];
+        y = r % e[1]; r /= e[1];
         z = (r < lo[2]) ? r : r + iz;
       } else if (q < cz + cy) {
         int r = q - cz;
-        int t = dv(r, f0);
-        x = r - t * e[0];
-        r = t;
-        t = dv(r, fwy);
-        const int yy = r - t * wy;
-        r = t;
+        x = r % e[0]; r /= e[0];
+        const int yy = r % wy; r /= wy;
         y = (yy < lo[1]) ? yy : yy + iy;
         z = lo[2] + r;
       } else {
         int r = q - cz - cy;
-        int t = dv(r, fwx);
-        const int xx = r - t * wx;
-        r = t;
+        const int xx = r % wx; r /= wx;
         x = (xx < lo[0]) ? xx : xx + (hi[0] - lo[0]);
-        t = dv(r, fiy);
-        y = lo[1] + (r - t * iy);
-        r = t;
+        y = lo[1] + r % iy; r /= iy;
         z = lo[2] + r;
       }
       int idx[3] = {x, y, z}, src[3], side[3];
