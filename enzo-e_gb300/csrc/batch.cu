@@ -29,10 +29,12 @@ namespace {
 
 __global__ void add_scalar_kernel(double* acc, const double* v) { *acc += *v; }
 
+// Work decomposition of one block-size class, per stage (0: half dt, NN;
+// 1: full dt, the configured reconstruction).
 struct TileChoice {
-  int tile_x = 0;  // x tile extent (0 = default)
-  int tile_y = 0;  // y tile extent (0 = default)
-  int zchunk = 0;  // z-chunk length (0 = whole block)
+  int tile_x[2] = {0, 0};  // x tile extent (0 = default)
+  int tile_y[2] = {0, 0};  // y tile extent (0 = default)
+  int zchunk[2] = {0, 0};  // z-chunk length (0 = whole block)
 };
 
 }  // namespace
@@ -69,7 +71,7 @@ struct mhdvlct_batch {
   double* d_diag = nullptr;   // diagnostics: partial rows then the 8 totals
   int diag_rows = 0;
   int grid = 0;               // persistent grid size (0 = fill the GPU)
-  int threads = 256;          // CTA size of the stage launches
+  int threads[2] = {256, 256};  // CTA size of each stage's launches
   std::map<std::vector<int>, TileChoice> tune;  // per block-size class
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   std::string err;
@@ -99,10 +101,12 @@ TileChoice choice_for(const mhdvlct_batch* b, int i) {
   auto it = b->tune.find(key);
   TileChoice c;
   if (it != b->tune.end()) c = it->second;
-  if (c.tile_x <= 0 || c.tile_y <= 0) {
-    const int t = default_tile(b->dtype, b->h->solver, b->h->recon, b->h->de);
-    c.tile_x = c.tile_y = t;
-  }
+  const StagePlan sp = stage_plan(b->h);
+  for (int s = 0; s < 2; s++)
+    if (c.tile_x[s] <= 0 || c.tile_y[s] <= 0) {
+      const int t = default_tile(b->dtype, b->h->solver, sp.recon[s], b->h->de);
+      c.tile_x[s] = c.tile_y[s] = t;
+    }
   return c;
 }
 
@@ -162,7 +166,7 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
     const TileChoice c = choice_for(b, i);
     for (int s = 0; s < 2; s++) {
       std::vector<StageTile> t;
-      make_tiles(i, O.m, sp.S[s], s == 1, c.tile_x, c.tile_y, c.zchunk, t);
+      make_tiles(i, O.m, sp.S[s], s == 1, c.tile_x[s], c.tile_y[s], c.zchunk[s], t);
       for (auto& x : t) {
         tx[s] = std::max(tx[s], x.xb - x.xa);
         ty[s] = std::max(ty[s], x.yb - x.ya);
@@ -224,7 +228,7 @@ cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
   info.tx = b->tile_tx[s];
   info.ty = b->tile_ty[s];
   info.queue = b->d_queue + s;
-  info.threads = b->threads;
+  info.threads = b->threads[s];
   return launch_stage<R>(b->h->solver, sp.recon[s], b->h->de != 0,
                          (const StageBlock<R>*)b->d_sblocks[b->parity][s],
                          b->d_tiles[s], b->ntiles[s], info, b->h->phys, b->grid, st);
@@ -512,8 +516,10 @@ extern "C" int mhdvlct_batch_set_tile(mhdvlct_batch* b, int tile_x, int tile_y) 
   for (int i = 0; i < b->nblocks; i++) {
     std::vector<int> key(b->dims.begin() + 3 * i, b->dims.begin() + 3 * i + 3);
     TileChoice c;
-    c.tile_x = tile_x;
-    c.tile_y = tile_y;
+    for (int s = 0; s < 2; s++) {
+      c.tile_x[s] = tile_x;
+      c.tile_y[s] = tile_y;
+    }
     b->tune[key] = c;
   }
   return build_descriptors_any(b, 0);
@@ -594,9 +600,9 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
   cudaEventCreate(&e1);
   json = "{";
   bool first_cls = true;
+  const StagePlan sp = stage_plan(b->h);
   for (const auto& cls : classes) {
     const int m_lat = std::max(cls[0], cls[1]) + 2 * b->g;
-    std::vector<TileChoice> cands;
     std::vector<std::pair<int, int>> shapes;
     for (int ty : {6, 8, 10, 12, 14, 16}) {
       for (int tx : {ty, (3 * ty) / 2, 2 * ty, 3 * ty, m_lat - 2, m_lat - 4})
@@ -605,33 +611,6 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
     }
     std::sort(shapes.begin(), shapes.end());
     shapes.erase(std::unique(shapes.begin(), shapes.end()), shapes.end());
-    // one launch serves every class, so its shared memory is sized by the
-    // largest tile extents over all classes: a candidate is kept only if that
-    // combined shape fits
-    int other_tx = 1, other_ty = 1;
-    for (int i = 0; i < b->nblocks; i++) {
-      if (b->dims[3 * i] == cls[0] && b->dims[3 * i + 1] == cls[1] &&
-          b->dims[3 * i + 2] == cls[2])
-        continue;
-      const TileChoice oc = choice_for(b, i);
-      other_tx = std::max(other_tx, oc.tile_x);
-      other_ty = std::max(other_ty, oc.tile_y);
-    }
-    for (auto& sh : shapes) {
-      if (stage_smem<R>(b->h->solver, b->h->recon, b->h->de != 0,
-                        std::max(sh.first, other_tx), std::max(sh.second, other_ty)) >
-          smem_cap)
-        continue;
-      for (int zc : {0, 16}) {
-        if (zc && zc >= cls[2]) continue;
-        TileChoice c;
-        c.tile_x = sh.first;
-        c.tile_y = sh.second;
-        c.zchunk = zc;
-        cands.push_back(c);
-      }
-    }
-    float best = 1e30f;
     int rep_block = 0;
     for (int i = 0; i < b->nblocks; i++)
       if (b->dims[3 * i] == cls[0] && b->dims[3 * i + 1] == cls[1] &&
@@ -640,48 +619,87 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
         break;
       }
     TileChoice bestc = choice_for(b, rep_block);
-    int best_threads = b->threads;
-    for (int threads : {256, 512}) {
-      if (threads > StageThreads<R>::max) continue;
-      b->threads = threads;
-      for (const auto& c : cands) {
-        b->tune[cls] = c;
-        if (int rc = build_descriptors<R>(b, st)) {
-          cudaFree(save);
-          return rc;
-        }
-        // one untimed step, then reps timed steps
-        e = launch_stages<R>(b, st);
-        cudaEventRecord(e0, st);
-        for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch_stages<R>(b, st);
-        cudaEventRecord(e1, st);
-        cudaEventSynchronize(e1);
-        cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
-        if (e == cudaErrorInvalidValue || e == cudaErrorInvalidConfiguration) {
-          // a launch shape this GPU refuses (nothing ran): skip the candidate
-          e = cudaSuccess;
+    float best_stage[2] = {0.f, 0.f};
+    size_t ncand = 0;
+    // the stages are tuned one after the other (each candidate is timed on
+    // the whole two-stage step, the other stage at its current choice)
+    for (int s = 0; s < 2; s++) {
+      // one launch serves every class, so its shared memory is sized by the
+      // largest tile extents over all classes: a candidate is kept only if
+      // that combined shape fits
+      int other_tx = 1, other_ty = 1;
+      for (int i = 0; i < b->nblocks; i++) {
+        if (b->dims[3 * i] == cls[0] && b->dims[3 * i + 1] == cls[1] &&
+            b->dims[3 * i + 2] == cls[2])
           continue;
-        }
-        if (e != cudaSuccess) break;
-        float t;
-        cudaEventElapsedTime(&t, e0, e1);
-        if (t < best) {
-          best = t;
-          bestc = c;
-          best_threads = threads;
+        const TileChoice oc = choice_for(b, i);
+        other_tx = std::max(other_tx, oc.tile_x[s]);
+        other_ty = std::max(other_ty, oc.tile_y[s]);
+      }
+      std::vector<TileChoice> cands;
+      for (auto& sh : shapes) {
+        if (stage_smem<R>(b->h->solver, sp.recon[s], b->h->de != 0,
+                          std::max(sh.first, other_tx), std::max(sh.second, other_ty)) >
+            smem_cap)
+          continue;
+        for (int zc : {0, 16}) {
+          if (zc && zc >= cls[2]) continue;
+          TileChoice c = bestc;
+          c.tile_x[s] = sh.first;
+          c.tile_y[s] = sh.second;
+          c.zchunk[s] = zc;
+          cands.push_back(c);
         }
       }
+      float best = 1e30f;
+      int best_threads = b->threads[s];
+      for (int threads : {256, 512}) {
+        if (threads > stage_max_threads<R>(sp.recon[s])) continue;
+        b->threads[s] = threads;
+        for (const auto& c : cands) {
+          ncand++;
+          b->tune[cls] = c;
+          if (int rc = build_descriptors<R>(b, st)) {
+            cudaFree(save);
+            return rc;
+          }
+          // one untimed step, then reps timed steps
+          e = launch_stages<R>(b, st);
+          cudaEventRecord(e0, st);
+          for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch_stages<R>(b, st);
+          cudaEventRecord(e1, st);
+          cudaEventSynchronize(e1);
+          cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
+          if (e == cudaErrorInvalidValue || e == cudaErrorInvalidConfiguration) {
+            // a launch shape this GPU refuses (nothing ran): skip the candidate
+            e = cudaSuccess;
+            continue;
+          }
+          if (e != cudaSuccess) break;
+          float t;
+          cudaEventElapsedTime(&t, e0, e1);
+          if (t < best) {
+            best = t;
+            bestc = c;
+            best_threads = threads;
+          }
+        }
+        if (e != cudaSuccess) break;
+      }
+      b->threads[s] = best_threads;
+      b->tune[cls] = bestc;
+      best_stage[s] = best / std::max(1, reps);
       if (e != cudaSuccess) break;
     }
-    b->threads = best_threads;
-    b->tune[cls] = bestc;
-    char buf[256];
+    char buf[512];
     std::snprintf(buf, sizeof(buf),
-                  "%s\"%dx%dx%d\": {\"tile_x\": %d, \"tile_y\": %d, \"zchunk\": %d, "
-                  "\"threads\": %d, \"ms_per_step\": %.4f, \"candidates\": %zu}",
-                  first_cls ? "" : ", ", cls[0], cls[1], cls[2], bestc.tile_x,
-                  bestc.tile_y, bestc.zchunk, b->threads, best / std::max(1, reps),
-                  2 * cands.size());
+                  "%s\"%dx%dx%d\": {\"stage1\": {\"tile_x\": %d, \"tile_y\": %d, "
+                  "\"zchunk\": %d, \"threads\": %d}, \"stage2\": {\"tile_x\": %d, "
+                  "\"tile_y\": %d, \"zchunk\": %d, \"threads\": %d}, "
+                  "\"ms_per_step\": %.4f, \"candidates\": %zu}",
+                  first_cls ? "" : ", ", cls[0], cls[1], cls[2], bestc.tile_x[0],
+                  bestc.tile_y[0], bestc.zchunk[0], b->threads[0], bestc.tile_x[1],
+                  bestc.tile_y[1], bestc.zchunk[1], b->threads[1], best_stage[1], ncand);
     json += buf;
     first_cls = false;
     if (e != cudaSuccess) break;

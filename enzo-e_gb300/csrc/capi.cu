@@ -102,9 +102,12 @@ template FieldSet<double> fieldset_of<double>(const MhdBlockView*);
 template FieldSet<float> fieldset_of<float>(const MhdBlockView*);
 
 int default_tile(int dtype, int solver, int recon, int de) {
-  // largest tile whose shared memory fits two CTAs' worth under 227 KB for
-  // FP32 and one CTA for FP64
-  const int cap = (dtype == MHD_DTYPE_F64) ? 200 * 1024 : 110 * 1024;
+  // largest tile whose shared memory fits the CTAs an SM holds at once
+  // (227 KB per SM): one CTA for FP64, three for the FP32 NN stage, two for
+  // the other FP32 stages
+  const int cap = (dtype == MHD_DTYPE_F64) ? 200 * 1024
+                  : (recon == RECON_NN)    ? 72 * 1024
+                                           : 110 * 1024;
   int best = 4;
   for (int t = 4; t <= (dtype == MHD_DTYPE_F64 ? TileLimits<double>::TMAX
                                                  : TileLimits<float>::TMAX);

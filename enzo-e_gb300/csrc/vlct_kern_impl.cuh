@@ -20,7 +20,8 @@ cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
       k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (nt <= 0) return cudaSuccess;
-  const int threads = (info.threads == 512 && StageThreads<R>::max >= 512) ? 512 : 256;
+  const int threads =
+      (info.threads == 512 && StageBounds<R, RECON>::threads >= 512) ? 512 : 256;
   if (grid <= 0) {
     // persistent grid: as many CTAs as fit on the GPU at once
     int dev = 0, nsm = 1, per_sm = 1;

@@ -109,14 +109,35 @@ size_t stage_smem_bytes(int tx, int ty) {
   return (size_t)L.total * sizeof(R);
 }
 
-// FP32: launched with 256 or 512 threads (the tuner's choice), registers
-// capped at 128 so that a 512-thread CTA fits an SM.  FP64: 256 threads with
-// up to 255 registers (the FP64 solver does not fit in 128 without spilling).
-template <class R> struct StageThreads { static constexpr int max = 256; };
-template <> struct StageThreads<float> { static constexpr int max = 512; };
+// Launch bounds per precision and reconstruction.  FP32 PLM: 256 or 512
+// threads (the tuner's choice), registers capped at 128 so that a 512-thread
+// CTA fits an SM.  FP32 NN (the half-dt stage, smaller ring and no slopes):
+// 256 threads, registers capped at 85 so that three CTAs share an SM.
+// FP64: 256 threads with up to 255 registers (the FP64 solver does not fit
+// in 128 without spilling).
+template <class R, int RECON> struct StageBounds {
+  static constexpr int threads = 256, min_blocks = 1;
+};
+template <> struct StageBounds<float, RECON_NN> {
+  static constexpr int threads = 256, min_blocks = 3;
+};
+template <> struct StageBounds<float, RECON_PLM> {
+  static constexpr int threads = 512, min_blocks = 1;
+};
+template <> struct StageBounds<float, RECON_PLM_ATHENA> {
+  static constexpr int threads = 512, min_blocks = 1;
+};
+// largest CTA a stage of this precision and reconstruction takes
+template <class R>
+inline int stage_max_threads(int recon) {
+  return recon == RECON_NN          ? StageBounds<R, RECON_NN>::threads
+         : recon == RECON_PLM       ? StageBounds<R, RECON_PLM>::threads
+                                    : StageBounds<R, RECON_PLM_ATHENA>::threads;
+}
 
 template <class R, int SOLVER, int RECON, bool DE>
-__global__ void __launch_bounds__(StageThreads<R>::max, 1)
+__global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
+                                  StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
              const StageTile* __restrict__ tiles, int ntiles, StageInfo info,
              PhysParams phys) {
