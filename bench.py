@@ -58,7 +58,7 @@ def _args():
     ap.add_argument("--cpu-sample-blocks", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mode", default="main",
-                    choices=["main", "amr", "serve", "precision"],
+                    choices=["main", "amr", "serve", "precision", "fc"],
                     help="main: the contract line; amr / serve / precision: the "
                          "mixed-size block set, the serving stream, the FP32-vs-FP64 "
                          "study (one JSON line each)")
@@ -67,7 +67,8 @@ def _args():
     ap.add_argument("--precision-n", type=int, default=512)
     ap.add_argument("--precision-cycles", type=int, default=50)
     ap.add_argument("--tile", type=str, default="",
-                    help="force the stage tile, e.g. 24x12 (skips the autotuner)")
+                    help="force the stage tiles, e.g. 24x12 or 30x10,28x14 (stage 1, "
+                         "stage 2; skips the autotuner)")
     return ap.parse_args()
 
 
@@ -466,6 +467,52 @@ def run_amr(a):
             "finite": all(np.isfinite(list(diag)))}
 
 
+def run_fc(a, nblocks=64, n=32):
+    """Flux correction on the plain per-block path: HLLC + PLM hydro blocks
+    (dual energy on), each advanced by timestep + compute, with and without
+    storing the dt/dx-scaled boundary fluxes of all six quantities."""
+    import numpy as np
+    import torch
+    from mhdvlct import block as B, serve as S
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", dual_energy=True,
+                               courant=COURANT)
+    out = {"mode": "fc", "workload": f"{nblocks} hydro blocks of {n}^3 (+{GHOST} ghosts), "
+                                     f"HLLC+PLM, dual energy, per-block Method calls"}
+    for dtype, tag in ((torch.float64, "f64"), (torch.float32, "f32")):
+        blocks = []
+        for i in range(nblocks):
+            st, box = S.request_state(n, 500 + i, 2.0, False)
+            st["internal_energy"] = (0.1 * st["density"]) / (
+                (5.0 / 3.0 - 1.0) * st["density"])
+            blk = B.Block((n, n, n), GHOST, (box / n,) * 3, mhd=False, dual_energy=True,
+                          dtype=dtype)
+            blk.load_numpy(st)
+            blocks.append(blk)
+        bufs = [B.FluxBuffers(blk, (0, 1, 2, 3, 4, 5)) for blk in blocks]
+        res = {}
+        for mode in ("plain", "store_fluxes"):
+            def cycle():
+                for blk, buf in zip(blocks, bufs):
+                    dt = meth.timestep(blk)
+                    if mode == "plain":
+                        meth.compute(blk, dt)
+                    else:
+                        meth.compute_store_fluxes(blk, dt, buffers=buf)
+            cycle()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(max(1, a.steps)):
+                cycle()
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+            res[mode] = nblocks * n ** 3 * max(1, a.steps) / el
+        out[tag] = {"plain_zone_updates_per_s": res["plain"],
+                    "store_fluxes_zone_updates_per_s": res["store_fluxes"],
+                    "overhead": res["plain"] / res["store_fluxes"] - 1.0}
+    return out
+
+
 class _DevArray:
     """A device buffer seen by torch through __cuda_array_interface__."""
 
@@ -606,6 +653,8 @@ def main():
                 out = run_amr(a)
             elif a.mode == "serve":
                 out = {"mode": "serve", **run_serve(nreq=a.serve_requests)}
+            elif a.mode == "fc":
+                out = run_fc(a)
             else:
                 out = run_precision(a, cycles=a.precision_cycles, N=a.precision_n)
             print(json.dumps(out), flush=True)
@@ -629,8 +678,11 @@ def main():
     h32 = make_batch(meth, blocks, widths, capi.MHD_DTYPE_F32, a.nb)
     tune = None
     if a.tile:
-        tx, ty = (int(v) for v in a.tile.lower().split("x"))
-        capi.check(L.mhdvlct_batch_set_tile(h32, tx, ty), meth.handle, "tile")
+        # "TXxTY" for both stages, or "TXxTY,TXxTY" for stage 1 and stage 2
+        for s_, spec in enumerate((a.tile.split(",") * 2)[:2]):
+            tx, ty = (int(v) for v in spec.lower().split("x"))
+            capi.check(L.mhdvlct_batch_set_stage_tile(h32, s_, tx, ty, 0, 256),
+                       meth.handle, "tile")
         tune = {"forced_tile": a.tile}
     elif not a.no_tune:
         buf = ctypes.create_string_buffer(4096)

@@ -525,6 +525,31 @@ extern "C" int mhdvlct_batch_set_tile(mhdvlct_batch* b, int tile_x, int tile_y) 
   return build_descriptors_any(b, 0);
 }
 
+extern "C" int mhdvlct_batch_set_stage_tile(mhdvlct_batch* b, int stage, int tile_x,
+                                            int tile_y, int zchunk, int threads) {
+  if (!b || stage < 0 || stage > 1 || tile_x < 0 || tile_y < 0 || zchunk < 0)
+    return MHD_ERR_INVALID;
+  const int tmax = b->dtype == MHD_DTYPE_F64 ? TileLimits<double>::TMAX
+                                             : TileLimits<float>::TMAX;
+  if (tile_x > tmax || tile_y > tmax) return bfail(b, MHD_ERR_INVALID, "tile too large");
+  const StagePlan sp = stage_plan(b->h);
+  const int tmax_threads = b->dtype == MHD_DTYPE_F64
+                               ? stage_max_threads<double>(sp.recon[stage])
+                               : stage_max_threads<float>(sp.recon[stage]);
+  if (threads != 0 && threads != 256 && !(threads == 512 && tmax_threads >= 512))
+    return bfail(b, MHD_ERR_INVALID, "threads must be 256 (or 512 where the stage allows it)");
+  for (int i = 0; i < b->nblocks; i++) {
+    std::vector<int> key(b->dims.begin() + 3 * i, b->dims.begin() + 3 * i + 3);
+    TileChoice c = choice_for(b, i);
+    c.tile_x[stage] = tile_x;
+    c.tile_y[stage] = tile_y;
+    c.zchunk[stage] = zchunk;
+    b->tune[key] = c;
+  }
+  b->threads[stage] = threads ? threads : 256;
+  return build_descriptors_any(b, 0);
+}
+
 extern "C" int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,
                                           size_t* bytes) {
   if (!b || !dev_ptr || !bytes) return MHD_ERR_INVALID;

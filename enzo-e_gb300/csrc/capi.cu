@@ -410,6 +410,7 @@ template <class R> struct PlainScratch {
   StageBlock<R>* d_sblocks;  // [2]
   AuxBlock<R>* d_aux;        // [1]
   int* d_nbr;                // [27]
+  void* d_fc;                // FluxOut<R> for the boundary fluxes
   StageTile* d_tiles;        // stage 0 tiles then stage 1 tiles
   int ntiles[2];
 };
@@ -441,6 +442,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   take(2 * sizeof(StageBlock<R>));
   take(sizeof(AuxBlock<R>));
   take(27 * sizeof(int));
+  take(sizeof(FluxOut<R>));
   take((tiles[0].size() + tiles[1].size()) * sizeof(StageTile));
   const bool same = h->scratch && h->cache_dtype == dtype && h->cache_m[0] == m[0] &&
                     h->cache_m[1] == m[1] && h->cache_m[2] == m[2] &&
@@ -471,6 +473,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   S.d_sblocks = (StageBlock<R>*)(base + offs[i++]);
   S.d_aux = (AuxBlock<R>*)(base + offs[i++]);
   S.d_nbr = (int*)(base + offs[i++]);
+  S.d_fc = (void*)(base + offs[i++]);
   S.d_tiles = (StageTile*)(base + offs[i++]);
   S.ntiles[0] = (int)tiles[0].size();
   S.ntiles[1] = (int)tiles[1].size();
@@ -492,7 +495,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
 
 template <class R>
 int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
-                 cudaStream_t st) {
+                 const MhdFluxCorrection* fc, cudaStream_t st) {
   const int g = b->ghost[0];
   const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
   PlainScratch<R> S;
@@ -536,6 +539,15 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   }
   e = cudaMemcpyAsync(S.d_sblocks, sb, sizeof(sb), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "block upload");
+  if (fc) {
+    FluxOut<R> fo;
+    for (int d = 0; d < 3; d++)
+      for (int sd = 0; sd < 2; sd++)
+        for (int q = 0; q < 6; q++) fo.f[d][sd][q] = (R*)fc->flux[d][sd][q];
+    fo.g = b->ghost[0];
+    e = cudaMemcpyAsync(S.d_fc, &fo, sizeof(fo), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "flux buffer upload");
+  }
   if (sp.nstages == 1) {
     for (int k = 0; k < NCELL; k++) {
       if (!ext.c[k]) continue;
@@ -554,6 +566,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     info.ty = h->tile;
     info.queue = nullptr;
     info.threads = 256;
+    if (fc && info.final_stage) info.fc = S.d_fc;
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, tiles[i],
                         S.ntiles[i], info, h->phys, 0, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");
@@ -624,8 +637,27 @@ extern "C" int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b,
   if (rc) return rc;
   if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
   cudaStream_t st = (cudaStream_t)stream;
-  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, st)
-                                   : block_step_t<float>(h, b, dt, st);
+  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, nullptr, st)
+                                   : block_step_t<float>(h, b, dt, nullptr, st);
+}
+
+extern "C" int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, double dt,
+                                     const MhdFluxCorrection* fc, void* stream) {
+  if (!h) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
+  if (!fc) return fail(h, MHD_ERR_INVALID, "null flux-correction buffers");
+  // EnzoMethodMHDVlct.cpp:136-141: flux corrections only in hydro mode
+  if (h->mhd)
+    return fail(h, MHD_ERR_INVALID, "Flux corrections are currently only supported in hydro-mode");
+  for (int d = 0; d < 3; d++)
+    for (int sd = 0; sd < 2; sd++)
+      if (fc->flux[d][sd][MHD_Q_INTERNAL_ENERGY] && !h->de)
+        return fail(h, MHD_ERR_INVALID, "internal_energy fluxes need dual energy");
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, fc, st)
+                                   : block_step_t<float>(h, b, dt, fc, st);
 }
 
 extern "C" int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,

@@ -52,6 +52,19 @@ struct StageInfo {
   int* queue;       // work counter (zeroed before the launch) for a persistent
                     // grid pulling tiles dynamically; null = static grid stride
   int threads;      // CTA size (256 or 512); 0 = 256
+  const void* fc = nullptr;  // FluxOut<R> (device) on the final stage when the
+                             // boundary fluxes are stored; null otherwise
+};
+
+// Boundary fluxes for flux correction (EnzoMethodMHDVlct.cpp:250-330):
+// f[dim][side][q] receives dt/dx_dim times the flux of quantity q (0 density,
+// 1-3 velocity x/y/z, 4 total energy, 5 internal energy) through the low
+// (side 0, face g-1) or high (side 1, face m-g-1) active face of axis dim,
+// as an array of the active face, last index fastest: axis 0 (nz, ny),
+// axis 1 (nz, nx), axis 2 (ny, nx).  Null pointers are skipped.
+template <class R> struct FluxOut {
+  R* f[3][2][6];
+  int g;
 };
 
 #ifdef __CUDACC__

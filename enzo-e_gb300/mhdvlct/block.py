@@ -130,6 +130,24 @@ def _stream_ptr(stream) -> int | None:
     return stream.cuda_stream
 
 
+class FluxBuffers:
+    """Device arrays of a block's boundary fluxes for flux correction:
+    arrays[(axis, side, quantity)] of the active face (axis 0: (nz, ny),
+    axis 1: (nz, nx), axis 2: (ny, nx)), in the block's dtype."""
+
+    def __init__(self, block: Block, quantities=(0, 1, 2, 3, 4)):
+        nx, ny, nz = block.n
+        shapes = [(nz, ny), (nz, nx), (ny, nx)]
+        self.fc = capi.MhdFluxCorrection()
+        self.arrays = {}
+        for ax in range(3):
+            for side in range(2):
+                for q in quantities:
+                    t = torch.zeros(shapes[ax], dtype=block.dtype, device=block.device)
+                    self.arrays[(ax, side, q)] = t
+                    self.fc.flux[ax][side][q] = t.data_ptr()
+
+
 class EnzoMethodMHDVlct:
     """The `mhd_vlct` Method on device-resident blocks."""
 
@@ -170,6 +188,22 @@ class EnzoMethodMHDVlct:
         rc = capi.lib().mhdvlct_block_step(self.handle, ctypes.byref(v), dt,
                                            _stream_ptr(stream))
         capi.check(rc, self.handle, "mhdvlct_block_step")
+
+    def compute_store_fluxes(self, block: Block, dt: float, quantities=(0, 1, 2, 3, 4),
+                             stream=None, buffers: "FluxBuffers | None" = None) -> dict:
+        """compute() with store_fluxes_for_corrections (hydro only,
+        EnzoMethodMHDVlct.cpp:250-330): returns {(axis, side, quantity):
+        device tensor} of dt/dx-scaled fluxes through the block's active
+        boundary faces.  Pass `buffers` (a FluxBuffers of this block's shape)
+        to reuse device arrays across calls."""
+        if buffers is None:
+            buffers = FluxBuffers(block, quantities)
+        v = block.view()
+        rc = capi.lib().mhdvlct_block_step_fc(self.handle, ctypes.byref(v), dt,
+                                              ctypes.byref(buffers.fc),
+                                              _stream_ptr(stream))
+        capi.check(rc, self.handle, "mhdvlct_block_step_fc")
+        return buffers.arrays
 
     def timestep(self, block: Block, stream=None) -> float:
         v = block.view()

@@ -28,12 +28,13 @@ EXPORTED = (
     "mhdvlct_params_default", "mhdvlct_params_parse", "mhdvlct_create",
     "mhdvlct_destroy", "mhdvlct_last_error_string",
     "mhdvlct_courant", "mhdvlct_required_ghost_depth", "mhdvlct_block_step",
-    "mhdvlct_block_step_noalloc",
+    "mhdvlct_block_step_noalloc", "mhdvlct_block_step_fc",
     "mhdvlct_block_timestep", "mhdvlct_fill_ghosts_periodic",
     "mhdvlct_batch_create", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
     "mhdvlct_batch_refresh", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
-    "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_autotune",
+    "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_set_stage_tile",
+    "mhdvlct_batch_autotune",
     "mhdvlct_batch_state_region", "mhdvlct_batch_profile",
     "mhdvlct_batch_diagnostics", "mhdserve_create",
     "mhdserve_destroy", "mhdserve_submit", "mhdserve_pump", "mhdserve_poll",
@@ -53,6 +54,15 @@ class MhdVlctParams(ctypes.Structure):
                 ("pressure_floor", ctypes.c_double),
                 ("dual_energy", ctypes.c_int),
                 ("dual_energy_eta", ctypes.c_double)]
+
+
+class MhdFluxCorrection(ctypes.Structure):
+    """flux[axis][side][quantity]: device arrays of the active boundary faces."""
+    _fields_ = [("flux", ctypes.c_void_p * 6 * 2 * 3)]
+
+
+MHD_Q_DENSITY, MHD_Q_VELOCITY_X, MHD_Q_VELOCITY_Y, MHD_Q_VELOCITY_Z = 0, 1, 2, 3
+MHD_Q_TOTAL_ENERGY, MHD_Q_INTERNAL_ENERGY = 4, 5
 
 
 class MhdBlockView(ctypes.Structure):
@@ -107,6 +117,7 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_courant.restype = dp
     L.mhdvlct_block_step.argtypes = [vp, P(MhdBlockView), dp, vp]
     L.mhdvlct_block_step_noalloc.argtypes = [vp, P(MhdBlockView), dp, vp]
+    L.mhdvlct_block_step_fc.argtypes = [vp, P(MhdBlockView), dp, P(MhdFluxCorrection), vp]
     L.mhdvlct_block_timestep.argtypes = [vp, P(MhdBlockView), P(dp), vp]
     L.mhdvlct_fill_ghosts_periodic.argtypes = [vp, P(MhdBlockView), vp]
     L.mhdvlct_batch_create.argtypes = [vp, P(ip), P(dp), ip, ip, ip, P(vp)]
@@ -121,6 +132,7 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_batch_autotune.argtypes = [vp, ip, ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mhdvlct_batch_state_region.argtypes = [vp, P(vp), P(ctypes.c_size_t)]
     L.mhdvlct_batch_profile.argtypes = [vp, ip, ip, P(ctypes.c_float), vp]
+    L.mhdvlct_batch_set_stage_tile.argtypes = [vp, ip, ip, ip, ip, ip]
     L.mhdvlct_batch_diagnostics.argtypes = [vp, P(dp), vp]
     L.mhdserve_create.argtypes = [P(MhdVlctParams), ctypes.c_size_t, ip, P(vp)]
     L.mhdserve_destroy.argtypes = [vp]

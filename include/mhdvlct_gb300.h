@@ -116,6 +116,29 @@ typedef struct MhdBlockView {
 int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b, double dt,
                        void* stream);
 
+/* Flux correction (store_fluxes_for_corrections, EnzoMethodMHDVlct.cpp:
+ * 136-141, 250-330, 483-490): the step additionally writes dt/dx_axis times
+ * the flux of selected integration quantities through the low (side 0, face
+ * between cells g-1 and g) and high (side 1, face between cells g+n-1 and
+ * g+n) active boundary of every axis, as Cello's FluxData holds them.
+ * flux[axis][side][quantity] is a device array of the block's active face in
+ * the block's dtype, last index fastest: axis 0 (nz, ny), axis 1 (nz, nx),
+ * axis 2 (ny, nx); NULL entries are skipped.  Hydro only (the reference
+ * asserts it); internal_energy needs dual energy. */
+enum {
+  MHD_Q_DENSITY = 0,
+  MHD_Q_VELOCITY_X = 1, /* the x-momentum flux, as the reference keys it */
+  MHD_Q_VELOCITY_Y = 2,
+  MHD_Q_VELOCITY_Z = 3,
+  MHD_Q_TOTAL_ENERGY = 4,
+  MHD_Q_INTERNAL_ENERGY = 5
+};
+typedef struct MhdFluxCorrection {
+  void* flux[3][2][6];
+} MhdFluxCorrection;
+int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, double dt,
+                          const MhdFluxCorrection* fc, void* stream);
+
 /* EnzoMethodMHDVlct::timestep (EnzoMethodMHDVlct.cpp:551-588): energy sync
  * (dual energy), pressure field, courant * CFL dt over the whole ghosted
  * block.  Synchronises `stream` to return dt on the host. */
@@ -182,6 +205,11 @@ int mhdvlct_batch_run(mhdvlct_batch* b, int ncycles, int dt_mode,
                       double* elapsed_time_out, void* stream);
 /* Work decomposition: tile extent used per block size class (0 = auto). */
 int mhdvlct_batch_set_tile(mhdvlct_batch* b, int tile_x, int tile_y);
+/* One stage's work decomposition for every block (stage 0: half dt, 1: full
+ * dt): tile extents, z-chunk length (0 = whole block) and CTA size (256, or
+ * 512 where the stage allows it; 0 = 256), e.g. to pin a tuned choice. */
+int mhdvlct_batch_set_stage_tile(mhdvlct_batch* b, int stage, int tile_x,
+                                 int tile_y, int zchunk, int threads);
 /* The autotuner: for every block-size class, time candidate (tile, z-chunk)
  * work decompositions on the batch's own data and keep the fastest.  The
  * state is restored afterwards.  json_out (may be NULL) receives a JSON

@@ -75,6 +75,11 @@ def ref_lib():
         L.ref_timestep.argtypes = [ctypes.POINTER(OracleParams),
                                    ctypes.POINTER(OracleBlock)]
         L.ref_timestep.restype = ctypes.c_double
+        L.ref_step_fc.argtypes = [ctypes.POINTER(OracleParams),
+                                  ctypes.POINTER(OracleBlock), ctypes.c_double,
+                                  ctypes.POINTER(_P), ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_int)]
+        L.ref_step_fc.restype = ctypes.c_int
         _ref = L
     return _ref
 
@@ -90,6 +95,11 @@ def lib():
         L.oracle_timestep.argtypes = [ctypes.POINTER(OracleParams),
                                       ctypes.POINTER(OracleBlock)]
         L.oracle_timestep.restype = ctypes.c_double
+        L.oracle_step_fc.argtypes = [ctypes.POINTER(OracleParams),
+                                     ctypes.POINTER(OracleBlock), ctypes.c_double,
+                                     ctypes.POINTER(_P), ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int)]
+        L.oracle_step_fc.restype = ctypes.c_int
         L.oracle_fill_ghosts_periodic.argtypes = [ctypes.POINTER(OracleBlock)]
         L.oracle_fill_ghosts_brick.argtypes = [ctypes.POINTER(OracleBlock),
                                                ctypes.c_int, ctypes.c_int,
@@ -167,6 +177,35 @@ def step(prm: OracleParams, b: Block, dt: float, ref: bool = False) -> None:
     rc = fn(ctypes.byref(prm), ctypes.byref(cs), dt)
     if rc != 0:
         raise RuntimeError(f"oracle_step failed: {rc}")
+
+
+FC_QUANTITIES = ("density", "velocity_x", "velocity_y", "velocity_z",
+                 "total_energy", "internal_energy")
+
+
+def step_fc(prm: OracleParams, b: Block, dt: float, quantities=(0, 1, 2, 3, 4),
+            ref: bool = False) -> dict:
+    """The step with store_fluxes_for_corrections; returns
+    {(dim, side, quantity): array} of dt/dx-scaled boundary fluxes
+    (EnzoMethodMHDVlct.cpp:250-330)."""
+    nx, ny, nz = b.n
+    shapes = [(nz, ny), (nz, nx), (ny, nx)]
+    nq = len(quantities)
+    arrs = {}
+    ptrs = (_P * (6 * nq))()
+    for dim in range(3):
+        for side in range(2):
+            for iq, q in enumerate(quantities):
+                a = np.zeros(shapes[dim])
+                arrs[(dim, side, q)] = a
+                ptrs[(dim * 2 + side) * nq + iq] = a.ctypes.data_as(_P)
+    qs = (ctypes.c_int * nq)(*quantities)
+    cs = b.cstruct()
+    fn = ref_lib().ref_step_fc if ref else lib().oracle_step_fc
+    rc = fn(ctypes.byref(prm), ctypes.byref(cs), dt, ptrs, nq, qs)
+    if rc != 0:
+        raise RuntimeError(f"step_fc failed: {rc}")
+    return arrs
 
 
 def timestep(prm: OracleParams, b: Block, ref: bool = False) -> float:

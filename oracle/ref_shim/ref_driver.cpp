@@ -129,7 +129,61 @@ struct Scratch {
 
 }  // namespace
 
+// The reference's own save_fluxes_for_corrections_ loop
+// (EnzoMethodMHDVlct.cpp:250-330), reading its flux maps after the final
+// stage; out and quantities as in oracle_step_fc.
+static void save_fc(const std::array<EnzoEFltArrayMap, 3>& flux_maps, int g,
+                    const int cc[3], const double cw[3], double dt,
+                    double* const* out, int nq, const int* quantities) {
+  static const char* names[6] = {"density", "velocity_x", "velocity_y",
+                                 "velocity_z", "total_energy", "internal_energy"};
+  const int n[3] = {cc[0] - 2 * g, cc[1] - 2 * g, cc[2] - 2 * g};
+  for (int dim = 0; dim < 3; dim++) {
+    const double dt_dxi = dt / cw[dim];
+    for (int iq = 0; iq < nq; iq++) {
+      CelloView<const enzo_float, 3> flux_arr = flux_maps[dim].at(names[quantities[iq]]);
+      double* left = out[(dim * 2 + 0) * nq + iq];
+      double* right = out[(dim * 2 + 1) * nq + iq];
+      if (dim == 0) {
+        const int left_ix = g - 1, right_ix = cc[0] - g - 1;
+        for (int iz = 0; iz < n[2]; iz++)
+          for (int iy = 0; iy < n[1]; iy++) {
+            if (left) left[iz * n[1] + iy] = dt_dxi * flux_arr(g + iz, g + iy, left_ix);
+            if (right) right[iz * n[1] + iy] = dt_dxi * flux_arr(g + iz, g + iy, right_ix);
+          }
+      } else if (dim == 1) {
+        const int left_iy = g - 1, right_iy = cc[1] - g - 1;
+        for (int iz = 0; iz < n[2]; iz++)
+          for (int ix = 0; ix < n[0]; ix++) {
+            if (left) left[iz * n[0] + ix] = dt_dxi * flux_arr(g + iz, left_iy, g + ix);
+            if (right) right[iz * n[0] + ix] = dt_dxi * flux_arr(g + iz, right_iy, g + ix);
+          }
+      } else {
+        const int left_iz = g - 1, right_iz = cc[2] - g - 1;
+        for (int iy = 0; iy < n[1]; iy++)
+          for (int ix = 0; ix < n[0]; ix++) {
+            if (left) left[iy * n[0] + ix] = dt_dxi * flux_arr(left_iz, g + iy, g + ix);
+            if (right) right[iy * n[0] + ix] = dt_dxi * flux_arr(right_iz, g + iy, g + ix);
+          }
+      }
+    }
+  }
+}
+
+static int ref_step_impl(const OracleParams* p, OracleBlock* b, double dt,
+                         double* const* fc_out, int fc_nq, const int* fc_q);
+
 extern "C" int ref_step(const OracleParams* p, OracleBlock* b, double dt) {
+  return ref_step_impl(p, b, dt, nullptr, 0, nullptr);
+}
+
+extern "C" int ref_step_fc(const OracleParams* p, OracleBlock* b, double dt,
+                           double* const* out, int nq, const int* quantities) {
+  return ref_step_impl(p, b, dt, out, nq, quantities);
+}
+
+static int ref_step_impl(const OracleParams* p, OracleBlock* b, double dt,
+                         double* const* fc_out, int fc_nq, const int* fc_q) {
   try {
     Setup s(p);
     Views views(b);
@@ -173,6 +227,11 @@ extern "C" int ref_step(const OracleParams* p, OracleBlock* b, double dt) {
           cur_dt, stale_depth, cw);
       stale_depth += s.integ->staling_from_stage(stage);
       if (bfield) bfield->increment_partial_timestep();
+      if (is_final && fc_out) {
+        const int cc[3] = {shape[2], shape[1], shape[0]};
+        const double cwd[3] = {b->dx, b->dy, b->dz};
+        save_fc(flux_maps, b->g, cc, cwd, dt, fc_out, fc_nq, fc_q);
+      }
     }
     delete bfield;
   } catch (const std::exception& e) {

@@ -960,8 +960,70 @@ long long g_flops = -1;
 
 extern "C" long long oracle_flop_count(void) { return g_flops; }
 
+// EnzoMethodMHDVlct::save_fluxes_for_corrections_ (EnzoMethodMHDVlct.cpp:
+// 250-330): after the final stage, dt/dx_dim times the flux through the low
+// (face g-1) and high (face m-g-1) active boundary of every axis, for the
+// requested integration quantities.  out[(dim * 2 + side) * nq + iq] holds an
+// array of the block's active face, last index fastest: axis 0 (nz, ny),
+// axis 1 (nz, nx), axis 2 (ny, nx).  quantities: 0 density, 1-3 velocity
+// x/y/z (the momentum flux), 4 total energy, 5 internal energy.
+static void save_boundary_fluxes(const Ctx& c, const Scratch& sc, double dt,
+                                 const double* cw, int g, double* const* out,
+                                 int nq, const int* quantities) {
+  const int* m = c.m;
+  const int n[3] = {m[0] - 2 * g, m[1] - 2 * g, m[2] - 2 * g};
+  for (int dim = 0; dim < 3; dim++) {
+    const double dt_dxi = dt / cw[dim];
+    for (int iq = 0; iq < nq; iq++) {
+      const int q = quantities[iq];
+      const V3 F = (q == 5) ? sc.eflux[dim].w
+                 : (q == 0) ? sc.flux[dim][Q_RHO].w
+                 : (q == 4) ? sc.flux[dim][Q_P].w
+                            : sc.flux[dim][Q_VX + (q - 1)].w;
+      for (int side = 0; side < 2; side++) {
+        double* dst = out[(dim * 2 + side) * nq + iq];
+        if (!dst) continue;
+        const int f = side == 0 ? g - 1 : m[dim] - g - 1;
+        if (dim == 0) {
+          for (int iz = 0; iz < n[2]; iz++)
+            for (int iy = 0; iy < n[1]; iy++)
+              dst[(size_t)iz * n[1] + iy] = dt_dxi * F.at(f, g + iy, g + iz);
+        } else if (dim == 1) {
+          for (int iz = 0; iz < n[2]; iz++)
+            for (int ix = 0; ix < n[0]; ix++)
+              dst[(size_t)iz * n[0] + ix] = dt_dxi * F.at(g + ix, f, g + iz);
+        } else {
+          for (int iy = 0; iy < n[1]; iy++)
+            for (int ix = 0; ix < n[0]; ix++)
+              dst[(size_t)iy * n[0] + ix] = dt_dxi * F.at(g + ix, g + iy, f);
+        }
+      }
+    }
+  }
+}
+
+static int step_impl(const OracleParams* p, OracleBlock* b, double dt,
+                     double* const* fc_out, int fc_nq, const int* fc_q);
+
 // EnzoMethodMHDVlct::compute (EnzoMethodMHDVlct.cpp:356-500)
 extern "C" int oracle_step(const OracleParams* p, OracleBlock* b, double dt) {
+  return step_impl(p, b, dt, nullptr, 0, nullptr);
+}
+
+// compute with store_fluxes_for_corrections (EnzoMethodMHDVlct.cpp:136-141,
+// :483-490): hydro only, as the reference asserts
+extern "C" int oracle_step_fc(const OracleParams* p, OracleBlock* b, double dt,
+                              double* const* out, int nq, const int* quantities) {
+  if (p->mhd) return 4;
+  for (int i = 0; i < nq; i++)
+    if (quantities[i] < 0 || quantities[i] > 5 ||
+        (quantities[i] == 5 && !p->dual_energy))
+      return 5;
+  return step_impl(p, b, dt, out, nq, quantities);
+}
+
+static int step_impl(const OracleParams* p, OracleBlock* b, double dt,
+                     double* const* fc_out, int fc_nq, const int* fc_q) {
   Ctx c;
   setup_ctx(c, p, b);
   const int* m = c.m;
@@ -1025,6 +1087,8 @@ extern "C" int oracle_step(const OracleParams* p, OracleBlock* b, double dt) {
     compute_update_stage(c, ext, cur, out, sc, fcur, face, fout, cw, recon,
                          cur_dt, stale);
     stale += staling_total(recon);
+    if (final_stage && fc_out)
+      save_boundary_fluxes(c, sc, dt, cw, b->g, fc_out, fc_nq, fc_q);
   }
   return 0;
 }

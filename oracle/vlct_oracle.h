@@ -44,6 +44,15 @@ typedef struct {
   double *pressure;                              /* [w] scratch field         */
 } OracleBlock;
 
+/* The step with store_fluxes_for_corrections (hydro only): after the final
+ * stage, out[(dim * 2 + side) * nq + iq] receives dt/dx_dim times the flux of
+ * quantity quantities[iq] (0 density, 1-3 velocity x/y/z, 4 total energy,
+ * 5 internal energy) through the low (side 0) or high (side 1) active face of
+ * axis dim, as arrays (nz, ny) / (nz, nx) / (ny, nx), last index fastest
+ * (EnzoMethodMHDVlct.cpp:250-330).  Returns 4 with magnetic fields. */
+int oracle_step_fc(const OracleParams* p, OracleBlock* b, double dt,
+                   double* const* out, int nq, const int* quantities);
+
 /* One full VL+CT step of size dt on one ghosted block, in place.  Returns 0,
  * or 3 for the euler scheme with magnetic fields (the reference ERRORs:
  * EnzoBfieldMethod.cpp:23-27). */

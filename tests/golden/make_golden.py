@@ -10,7 +10,9 @@ records:
   - the reference dt (`EnzoMethodMHDVlct::timestep`, as a float hex string);
   - the SHA-256 of every field after the timestep call and one
     `EnzoMethodMHDVlct::compute` step of that dt;
-  - the density after the step as a raw array.
+  - the density after the step as a raw array;
+  - for hydro cases, the SHA-256 of every boundary-flux array the step
+    stores for flux correction (store_fluxes_for_corrections).
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -27,6 +29,9 @@ sys.path.insert(0, HERE)
 
 from oracle import oracle as O  # noqa: E402
 from golden_input import CASES, G, N, WIDTHS, digest, golden_input  # noqa: E402
+
+FC_QUANTITIES = (0, 1, 2, 3, 4)
+FC_QUANTITIES_DE = (0, 1, 2, 3, 4, 5)
 
 ORACLE_NAME = {"density": "rho", "velocity_x": "vx", "velocity_y": "vy",
                "velocity_z": "vz", "total_energy": "etot",
@@ -67,7 +72,16 @@ def main():
         b = oracle_block(state, mhd, de)
         prm = case_params(solver, recon, de, scheme, theta)
         dt = O.timestep(prm, b, ref=True)
-        O.step(prm, b, dt, ref=True)
+        if mhd:
+            O.step(prm, b, dt, ref=True)
+        else:
+            # hydro: the step also stores the boundary fluxes for flux
+            # correction (EnzoMethodMHDVlct.cpp:250-330)
+            qs = FC_QUANTITIES_DE if de else FC_QUANTITIES
+            fc = O.step_fc(prm, b, dt, qs, ref=True)
+            rec["fc_quantities"] = list(qs)
+            rec["fc_sha256"] = {f"{ax}{side}{q}": digest(a)
+                                for (ax, side, q), a in sorted(fc.items())}
         rec["dt"] = float(dt).hex()
         rec["output_sha256"] = {k: digest(b.f[ORACLE_NAME[k]]) for k in sorted(state)}
         out["cases"][name] = rec

@@ -56,3 +56,30 @@ def test_oracle_rejects_euler_with_constrained_transport():
     prm = oracle_params("hlld", "nn", euler=True, courant=1.0)
     with pytest.raises(RuntimeError):
         O.step(prm, b, 1e-3)
+
+
+FC_CASES = [c for c in CASES if "fc_sha256" in GOLD["cases"][c[0]]]
+
+
+@pytest.mark.parametrize("case", FC_CASES, ids=[c[0] for c in FC_CASES])
+def test_oracle_boundary_fluxes_match_reference_golden(case):
+    """store_fluxes_for_corrections: the dt/dx-scaled fluxes through the
+    active boundary faces equal the reference's bit for bit."""
+    name, solver, recon, de, scheme, theta, seed = case
+    rec = GOLD["cases"][name]
+    state = golden_input(N, G, seed, mhd=False, dual_energy=de)
+    b = oracle_block(state, N, G, WIDTHS, mhd=False, de=de)
+    prm = oracle_params(solver, recon, de=de, euler=scheme == "euler", theta=theta,
+                        courant=1.0 if scheme == "euler" else 0.3)
+    dt = O.timestep(prm, b)
+    fc = O.step_fc(prm, b, dt, tuple(rec["fc_quantities"]))
+    got = {f"{ax}{side}{q}": digest(a) for (ax, side, q), a in sorted(fc.items())}
+    assert got == rec["fc_sha256"]
+    assert np.array_equal(b.f["rho"], DENS[name])
+
+
+def test_oracle_flux_correction_rejects_mhd():
+    state = golden_input(N, G, 1, mhd=True)
+    b = oracle_block(state, N, G, WIDTHS, mhd=True)
+    with pytest.raises(RuntimeError):
+        O.step_fc(oracle_params("hlld", "plm"), b, 1e-3)

@@ -55,3 +55,24 @@ def test_fp32_within_tolerance_of_reference_golden(case):
     dt_ref = float.fromhex(rec["dt"])
     assert abs(dt - dt_ref) / dt_ref < 1e-6
     assert rel_l1(out["density"].astype(np.float64), DENS[case[0]]) <= 1e-5
+
+
+FC_CASES = [c for c in CASES if "fc_sha256" in GOLD["cases"][c[0]]]
+
+
+@pytest.mark.parametrize("case", FC_CASES, ids=[c[0] for c in FC_CASES])
+def test_fp64_boundary_fluxes_match_reference_golden(case):
+    name, solver, recon, de, scheme, theta, seed = case
+    rec = GOLD["cases"][name]
+    state = golden_input(N, G, seed, mhd=False, dual_energy=de)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver=solver,
+                               reconstruct_method=recon, time_scheme=scheme,
+                               dual_energy=de, theta_limiter=theta)
+    blk = B.Block(N, G, WIDTHS, mhd=False, dual_energy=de, dtype=torch.float64)
+    blk.load_numpy(state)
+    dt = meth.timestep(blk)
+    fc = meth.compute_store_fluxes(blk, dt, tuple(rec["fc_quantities"]))
+    torch.cuda.synchronize()
+    got = {f"{ax}{side}{q}": digest(t.cpu().numpy()) for (ax, side, q), t in sorted(fc.items())}
+    assert got == rec["fc_sha256"]
+    assert digest(blk.to_numpy()["density"]) == rec["output_sha256"]["density"]
