@@ -392,6 +392,10 @@ int check_view(mhdvlct_handle* h, const MhdBlockView* b) {
       if (!b->bfield[d] || !b->bfieldi[d])
         return fail(h, MHD_ERR_INVALID, "missing bfield / bfieldi pointer");
   }
+  const int nacc = (b->acceleration[0] != nullptr) + (b->acceleration[1] != nullptr) +
+                   (b->acceleration[2] != nullptr);
+  if (nacc != 0 && nacc != 3)
+    return fail(h, MHD_ERR_INVALID, "give all three acceleration fields or none");
   return MHD_OK;
 }
 
@@ -520,6 +524,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     B.dt = S.d_dt;
     const bool final = (i + 1) == sp.nstages;
     B.base = ext;
+    for (int d = 0; d < 3; d++) B.accel[d] = (const R*)b->acceleration[d];
     if (sp.nstages == 1) {
       // euler: a single stage cannot update its own input in place, so it
       // reads a copy of the block and writes into the caller's fields
@@ -566,6 +571,9 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     info.ty = h->tile;
     info.queue = nullptr;
     info.threads = 256;
+    // EnzoMHDIntegratorStageCommands.cpp:279: the gravity source enters the
+    // stage with index 1 (the full-dt stage of vl; never with euler)
+    info.gravity = (i == 1 && b->acceleration[0] != nullptr) ? 1 : 0;
     if (fc && info.final_stage) info.fc = S.d_fc;
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, tiles[i],
                         S.ntiles[i], info, h->phys, 0, st);
@@ -825,6 +833,7 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     }
     B.dt = S.d_dt;
     B.base = ext;
+    for (int d = 0; d < 3; d++) B.accel[d] = (const R*)b->acceleration[d];
     if (sp.nstages == 1) {
       B.cur = tmp;
       for (int d = 0; d < 3; d++) B.cur.f[d] = ext.f[d];
@@ -869,6 +878,9 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     info.ty = h->tile;
     info.queue = nullptr;
     info.threads = 256;
+    // EnzoMHDIntegratorStageCommands.cpp:279: the gravity source enters the
+    // stage with index 1 (the full-dt stage of vl; never with euler)
+    info.gravity = (i == 1 && b->acceleration[0] != nullptr) ? 1 : 0;
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, dtiles[i],
                         ntiles[i], info, h->phys, 0, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");

@@ -172,6 +172,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
 
   __shared__ int s_next;
   __shared__ R s_dtdx[3];
+  __shared__ R s_dt;
   int it = blockIdx.x;
   if (info.queue) {
     if (tid == 0) s_next = atomicAdd(info.queue, 1);
@@ -190,6 +191,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
       s_dtdx[0] = R(dt / B.cw[0]);
       s_dtdx[1] = R(dt / B.cw[1]);
       s_dtdx[2] = R(dt / B.cw[2]);
+      s_dt = R(dt);
     }
     __syncthreads();
     const R dtdx[3] = {s_dtdx[0], s_dtdx[1], s_dtdx[2]};
@@ -587,6 +589,19 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
             a -= dtdx[2] * (zfp[S_EINT * G + r] - zfm[S_EINT * G + r]);
             a -= dtdx[2] * p * (zfp[S_VBAR * G + r] - zfm[S_VBAR * G + r]);
             du[5] = a;
+          }
+          // gravity source on the full-dt stage (EnzoSourceGravity.cpp:17-69,
+          // EnzoMHDIntegratorStageCommands.cpp:267-297): start-of-step
+          // density and velocity
+          if (info.gravity) {
+            const R dt = s_dt;
+            const R rho0 = B.base.c[F_RHO][c];
+            const R ax = B.accel[0][c], ay = B.accel[1][c], az = B.accel[2][c];
+            du[1] += dt * rho0 * ax;
+            du[2] += dt * rho0 * ay;
+            du[3] += dt * rho0 * az;
+            du[4] += dt * rho0 * ((B.base.c[F_VX][c] * ax) + (B.base.c[F_VY][c] * ay) +
+                                  (B.base.c[F_VZ][c] * az));
           }
           // update_quantities (EnzoIntegrationQuanUpdate.cpp:183-231)
           const R old_rho = B.base.c[F_RHO][c];

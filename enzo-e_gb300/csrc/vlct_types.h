@@ -24,6 +24,7 @@ template <class R> struct StageBlock {
   FieldSet<R> cur;       // state the fluxes are computed from
   FieldSet<R> base;      // start-of-step state (U^n, face B^n)
   FieldSet<R> out;       // where the stage writes (out.f = new face B)
+  const R* accel[3] = {nullptr, nullptr, nullptr};  // gravity source fields
 };
 
 // One unit of work: a column tile [xa, xb) x [ya, yb) of one block, whose
@@ -52,6 +53,7 @@ struct StageInfo {
   int* queue;       // work counter (zeroed before the launch) for a persistent
                     // grid pulling tiles dynamically; null = static grid stride
   int threads;      // CTA size (256 or 512); 0 = 256
+  int gravity = 0;           // 1: add the gravity source (the blocks' accel)
   const void* fc = nullptr;  // FluxOut<R> (device) on the final stage when the
                              // boundary fluxes are stored; null otherwise
 };

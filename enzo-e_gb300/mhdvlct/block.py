@@ -29,7 +29,8 @@ class Block:
     along axis d (src/Cello/data_FieldData.cpp:585-619)."""
 
     def __init__(self, n, ghost=3, cell_width=(1.0, 1.0, 1.0), mhd=True,
-                 dual_energy=False, dtype=torch.float64, device="cuda"):
+                 dual_energy=False, dtype=torch.float64, device="cuda",
+                 gravity=False):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
         self.n = (int(nx), int(ny), int(nz))
         self.ghost = int(ghost)
@@ -46,6 +47,8 @@ class Block:
                 "total_energy", "pressure"]
         if dual_energy:
             keys.append("internal_energy")
+        if gravity:
+            keys += ["acceleration_x", "acceleration_y", "acceleration_z"]
         if mhd:
             keys += ["bfield_x", "bfield_y", "bfield_z"]
         self.fields = {k: torch.zeros(shp, dtype=dtype, device=device)
@@ -80,6 +83,8 @@ class Block:
         for a, k in enumerate(FACE_KEYS):
             v.bfieldi[a] = p(k)
         v.pressure = p("pressure")
+        for a, k in enumerate(("acceleration_x", "acceleration_y", "acceleration_z")):
+            v.acceleration[a] = p(k)
         return v
 
     # host <-> device helpers (tests, IC upload)

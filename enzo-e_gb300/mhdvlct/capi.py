@@ -76,7 +76,8 @@ class MhdBlockView(ctypes.Structure):
                 ("internal_energy", ctypes.c_void_p),
                 ("bfield", ctypes.c_void_p * 3),
                 ("bfieldi", ctypes.c_void_p * 3),
-                ("pressure", ctypes.c_void_p)]
+                ("pressure", ctypes.c_void_p),
+                ("acceleration", ctypes.c_void_p * 3)]
 
 
 class MhdServeRequest(ctypes.Structure):

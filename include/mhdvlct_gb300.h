@@ -109,6 +109,10 @@ typedef struct MhdBlockView {
   void* bfield[3];        /* cell-centred bfield_x/y/z (MHD only)            */
   void* bfieldi[3];       /* face-centred bfieldi_x/y/z (MHD only)           */
   void* pressure;         /* [w] pressure field; may be NULL                 */
+  void* acceleration[3];  /* acceleration_x/y/z for the gravity source term
+                           * (EnzoSourceGravity.cpp:17-69, applied on the
+                           * full-dt stage of the vl scheme); all three or
+                           * none (NULL)                                      */
 } MhdBlockView;
 
 /* EnzoMethodMHDVlct::compute (EnzoMethodMHDVlct.cpp:356-500): one VL+CT step

@@ -43,7 +43,7 @@ class OracleBlock(ctypes.Structure):
                 ("dy", ctypes.c_double), ("dz", ctypes.c_double)] + [
                     (n, _P) for n in ("rho", "vx", "vy", "vz", "etot", "eint",
                                       "bx", "by", "bz", "bfx", "bfy", "bfz",
-                                      "pressure")]
+                                      "pressure", "ax", "ay", "az")]
 
 
 def build(force: bool = False) -> str:
@@ -128,7 +128,7 @@ class Block:
     """One ghosted block held as float64 numpy arrays in Cello's layout."""
 
     def __init__(self, n, g=3, widths=(1.0, 1.0, 1.0), mhd=True,
-                 dual_energy=False):
+                 dual_energy=False, gravity=False):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else n
         self.n = (nx, ny, nz)
         self.g = g
@@ -143,6 +143,9 @@ class Block:
             self.f[k] = np.zeros(shp)
         if dual_energy:
             self.f["eint"] = np.zeros(shp)
+        if gravity:
+            for k in ("ax", "ay", "az"):
+                self.f[k] = np.zeros(shp)
         if mhd:
             for k in ("bx", "by", "bz"):
                 self.f[k] = np.zeros(shp)
@@ -168,7 +171,8 @@ class Block:
         return OracleBlock(nx, ny, nz, self.g, dx, dy, dz,
                            *[p(k) for k in ("rho", "vx", "vy", "vz", "etot",
                                             "eint", "bx", "by", "bz", "bfx",
-                                            "bfy", "bfz", "pressure")])
+                                            "bfy", "bfz", "pressure", "ax",
+                                            "ay", "az")])
 
 
 def step(prm: OracleParams, b: Block, dt: float, ref: bool = False) -> None:

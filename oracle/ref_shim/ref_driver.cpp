@@ -92,6 +92,9 @@ struct Views {
     put("bfieldi_y", b->bfy, 0, 1, 0);
     put("bfieldi_z", b->bfz, 0, 0, 1);
     put("pressure", b->pressure, 0, 0, 0);
+    put("acceleration_x", b->ax, 0, 0, 0);
+    put("acceleration_y", b->ay, 0, 0, 0);
+    put("acceleration_z", b->az, 0, 0, 0);
   }
   EnzoEFltArrayMap map(const str_vec_t& keys) {
     std::vector<EFlt3DArray> arrs;
@@ -205,7 +208,12 @@ static int ref_step_impl(const OracleParams* p, OracleBlock* b, double dt,
                     de);
     std::array<EnzoEFltArrayMap, 3> flux_maps = {
         scratch.xflux_map, scratch.yflux_map, scratch.zflux_map};
-    const EnzoEFltArrayMap accel_map;
+    // get_accel_map_ (EnzoMethodMHDVlct.cpp:219-233): empty without the
+    // acceleration fields
+    const EnzoEFltArrayMap accel_map =
+        (b->ax && b->ay && b->az)
+            ? views.map({"acceleration_x", "acceleration_y", "acceleration_z"})
+            : EnzoEFltArrayMap();
     EFlt3DArray interface_vel_arr = scratch.interface_vel_arr;
     const int nstages = p->euler ? 1 : 2;
     EnzoBfieldMethod* bfield = s.integ->construct_bfield_method(nstages);

@@ -89,6 +89,8 @@ struct Ctx {
   int m[3];  // ghosted cell extent along x, y, z
   bool mhd, de;
   double gamma;
+  bool gravity = false;  // acceleration fields present
+  V3 accel[3];
 };
 
 /* ------------------------------------------------------------------------ */
@@ -896,11 +898,33 @@ int staling_total(int recon) { return recon == ORC_NN ? 1 : 2; }
 int staling_immediate(int recon) { return recon == ORC_NN ? 0 : 1; }
 
 // EnzoMHDIntegratorStageCommands::compute_update_stage (:102-203)
+// EnzoSourceGravity::calculate_source (toolkit/EnzoSourceGravity.cpp:17-69):
+// momentum and energy sources from the acceleration fields, with the density
+// and velocity of the start of the timestep
+void gravity_source(const Ctx& c, const Integ& begin, Scratch& sc, double dt,
+                    int stale) {
+  const V3 dmx = sc.dU[1].w, dmy = sc.dU[2].w, dmz = sc.dU[3].w, dE = sc.dU[4].w;
+  for (int iz = stale; iz < c.m[2] - stale; iz++)
+    for (int iy = stale; iy < c.m[1] - stale; iy++)
+      for (int ix = stale; ix < c.m[0] - stale; ix++) {
+        const double rho = begin.rho.at(ix, iy, iz);
+        const double ax = c.accel[0].at(ix, iy, iz);
+        const double ay = c.accel[1].at(ix, iy, iz);
+        const double az = c.accel[2].at(ix, iy, iz);
+        dmx.at(ix, iy, iz) += dt * rho * ax;
+        dmy.at(ix, iy, iz) += dt * rho * ay;
+        dmz.at(ix, iy, iz) += dt * rho * az;
+        dE.at(ix, iy, iz) += dt * rho * ((begin.vx.at(ix, iy, iz) * ax) +
+                                         (begin.vy.at(ix, iy, iz) * ay) +
+                                         (begin.vz.at(ix, iy, iz) * az));
+      }
+}
+
 void compute_update_stage(const Ctx& c, const Integ& begin, const Integ& cur,
                           const Integ& out, Scratch& sc, const V3* face_cur,
                           const V3* face_base, const V3* face_out,
                           const double* cw, int recon, double cur_dt,
-                          int stale) {
+                          int stale, bool full_timestep) {
   for (int k = 0; k < 6; k++) std::fill(sc.dU[k].v.begin(), sc.dU[k].v.end(), 0.0);
   primitive_from_integration(c, cur, sc, stale);
   for (int dim = 0; dim < 3; dim++) {
@@ -912,6 +936,9 @@ void compute_update_stage(const Ctx& c, const Integ& begin, const Integ& cur,
     if (c.mhd) identify_upwind(c, sc, dim, cs);
   }
   stale += staling_immediate(recon);
+  // compute_source_terms_ (EnzoMHDIntegratorStageCommands.cpp:267-297):
+  // gravity on the full-timestep stage (stage index 1) only
+  if (full_timestep && c.gravity) gravity_source(c, begin, sc, cur_dt, stale);
   if (c.mhd) {
     // update_all_bfield_components (EnzoBfieldMethodCT.cpp:220-263)
     edge_efields(c, sc, cur, stale);
@@ -948,6 +975,12 @@ void setup_ctx(Ctx& c, const OracleParams* p, const OracleBlock* b) {
   c.mhd = p->mhd != 0;
   c.de = p->dual_energy != 0;
   c.gamma = p->gamma;
+  c.gravity = b->ax && b->ay && b->az;
+  if (c.gravity) {
+    c.accel[0] = view(b->ax, c.m[0], c.m[1], c.m[2]);
+    c.accel[1] = view(b->ay, c.m[0], c.m[1], c.m[2]);
+    c.accel[2] = view(b->az, c.m[0], c.m[1], c.m[2]);
+  }
 }
 
 long long g_flops = -1;
@@ -1085,7 +1118,7 @@ static int step_impl(const OracleParams* p, OracleBlock* b, double dt,
     const V3* fcur = (st == 0) ? face : tface;
     const V3* fout = final_stage ? face : tface;
     compute_update_stage(c, ext, cur, out, sc, fcur, face, fout, cw, recon,
-                         cur_dt, stale);
+                         cur_dt, stale, st == 1);
     stale += staling_total(recon);
     if (final_stage && fc_out)
       save_boundary_fluxes(c, sc, dt, cw, b->g, fc_out, fc_nq, fc_q);

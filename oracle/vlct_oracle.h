@@ -42,6 +42,7 @@ typedef struct {
   double *bx, *by, *bz;                          /* cell-centred B (MHD)      */
   double *bfx, *bfy, *bfz;                       /* face-centred B (MHD)      */
   double *pressure;                              /* [w] scratch field         */
+  double *ax, *ay, *az;  /* acceleration_x/y/z (gravity source), or NULL     */
 } OracleBlock;
 
 /* The step with store_fluxes_for_corrections (hydro only): after the final
