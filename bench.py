@@ -686,7 +686,7 @@ def main():
         tune = {"forced_tile": a.tile}
     elif not a.no_tune:
         buf = ctypes.create_string_buffer(4096)
-        capi.check(L.mhdvlct_batch_autotune(h32, 2, buf, 4096, sp), meth.handle,
+        capi.check(L.mhdvlct_batch_autotune(h32, 4, buf, 4096, sp), meth.handle,
                    "autotune")
         tune = json.loads(buf.value.decode() or "{}")
     tsim = ctypes.c_double()

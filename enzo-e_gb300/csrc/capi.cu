@@ -396,6 +396,10 @@ int check_view(mhdvlct_handle* h, const MhdBlockView* b) {
                    (b->acceleration[2] != nullptr);
   if (nacc != 0 && nacc != 3)
     return fail(h, MHD_ERR_INVALID, "give all three acceleration fields or none");
+  if (b->npassive < 0 || b->npassive > 4)
+    return fail(h, MHD_ERR_INVALID, "npassive must be in [0, 4]");
+  for (int k = 0; k < b->npassive; k++)
+    if (!b->passive[k]) return fail(h, MHD_ERR_INVALID, "missing passive scalar pointer");
   return MHD_OK;
 }
 
@@ -406,6 +410,7 @@ int cuda_fail(mhdvlct_handle* h, cudaError_t e, const char* where) {
 // Scratch of the plain path, carved from one allocation.
 template <class R> struct PlainScratch {
   R* tmp[NCELL];
+  R* tpass[4];               // half-step passive scalars
   R* tface[3];
   R* fface[3];
   double* d_dt;
@@ -423,7 +428,7 @@ size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
 template <class R>
 int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
-                   PlainScratch<R>& S, cudaStream_t st) {
+                   PlainScratch<R>& S, cudaStream_t st, int np = 0) {
   const StagePlan sp = stage_plan(h);
   if (h->tile <= 0) h->tile = 8;
   std::vector<StageTile> tiles[2];
@@ -440,6 +445,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   for (int k = 0; k < NCELL; k++) take(M * sizeof(R));
   for (int d = 0; d < 3; d++) take(F[d] * sizeof(R));
   for (int d = 0; d < 3; d++) take(F[d] * sizeof(R));
+  for (int k = 0; k < np; k++) take(M * sizeof(R));
   take(sizeof(double));
   take(sizeof(double));
   take(3 * sizeof(unsigned long long));
@@ -450,7 +456,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   take((tiles[0].size() + tiles[1].size()) * sizeof(StageTile));
   const bool same = h->scratch && h->cache_dtype == dtype && h->cache_m[0] == m[0] &&
                     h->cache_m[1] == m[1] && h->cache_m[2] == m[2] &&
-                    h->scratch_bytes >= off;
+                    h->cache_np == np && h->scratch_bytes >= off;
   if (!same) {
     if (h->scratch) {
       cudaStreamSynchronize(st);
@@ -464,6 +470,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
     }
     h->scratch_bytes = off;
     h->cache_dtype = dtype;
+    h->cache_np = np;
     for (int a = 0; a < 3; a++) h->cache_m[a] = m[a];
   }
   char* base = (char*)h->scratch;
@@ -471,6 +478,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   for (int k = 0; k < NCELL; k++) S.tmp[k] = (R*)(base + offs[i++]);
   for (int d = 0; d < 3; d++) S.tface[d] = (R*)(base + offs[i++]);
   for (int d = 0; d < 3; d++) S.fface[d] = (R*)(base + offs[i++]);
+  for (int k = 0; k < 4; k++) S.tpass[k] = k < np ? (R*)(base + offs[i++]) : nullptr;
   S.d_dt = (double*)(base + offs[i++]);
   S.d_dtout = (double*)(base + offs[i++]);
   S.d_smax = (void*)(base + offs[i++]);
@@ -491,7 +499,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
     e = cudaMemcpyAsync(S.d_nbr, nbr.data(), 27 * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "neighbour upload");
     // scratch cell fields that a block never writes must still be defined
-    e = cudaMemsetAsync(h->scratch, 0, offs[NCELL + 6], st);
+    e = cudaMemsetAsync(h->scratch, 0, offs[NCELL + 6 + np], st);
     if (e != cudaSuccess) return cuda_fail(h, e, "scratch clear");
   }
   return MHD_OK;
@@ -503,7 +511,8 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   const int g = b->ghost[0];
   const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
   PlainScratch<R> S;
-  int rc = ensure_scratch<R>(h, m, b->dtype, S, st);
+  const int np = b->npassive;
+  int rc = ensure_scratch<R>(h, m, b->dtype, S, st, np);
   if (rc) return rc;
   const StagePlan sp = stage_plan(h);
   FieldSet<R> ext = fieldset_of<R>(b);
@@ -525,6 +534,15 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     const bool final = (i + 1) == sp.nstages;
     B.base = ext;
     for (int d = 0; d < 3; d++) B.accel[d] = (const R*)b->acceleration[d];
+    for (int k = 0; k < np; k++) {
+      R* ep = (R*)b->passive[k];
+      B.pass_base[k] = ep;
+      // vl: stage 0 reads the caller's scalars and writes the half step,
+      // stage 1 reads the half step and writes the caller's; euler reads a
+      // copy (made below) and writes the caller's
+      B.pass_cur[k] = (sp.nstages == 1 || i == 1) ? S.tpass[k] : ep;
+      B.pass_out[k] = (sp.nstages == 2 && i == 0) ? S.tpass[k] : ep;
+    }
     if (sp.nstages == 1) {
       // euler: a single stage cannot update its own input in place, so it
       // reads a copy of the block and writes into the caller's fields
@@ -559,6 +577,11 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
       e = cudaMemcpyAsync(S.tmp[k], ext.c[k], M * sizeof(R), cudaMemcpyDeviceToDevice, st);
       if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
     }
+    for (int k = 0; k < np; k++) {
+      e = cudaMemcpyAsync(S.tpass[k], b->passive[k], M * sizeof(R), cudaMemcpyDeviceToDevice,
+                          st);
+      if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
+    }
   }
   const StageTile* tiles[2] = {S.d_tiles, S.d_tiles + S.ntiles[0]};
   for (int i = 0; i < sp.nstages; i++) {
@@ -574,6 +597,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     // EnzoMHDIntegratorStageCommands.cpp:279: the gravity source enters the
     // stage with index 1 (the full-dt stage of vl; never with euler)
     info.gravity = (i == 1 && b->acceleration[0] != nullptr) ? 1 : 0;
+    info.npass = np;
     if (fc && info.final_stage) info.fc = S.d_fc;
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, tiles[i],
                         S.ntiles[i], info, h->phys, 0, st);
@@ -593,7 +617,7 @@ int aux_setup(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
               cudaStream_t st) {
   const int g = b->ghost[0];
   const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
-  int rc = ensure_scratch<R>(h, m, b->dtype, S, st);
+  int rc = ensure_scratch<R>(h, m, b->dtype, S, st, b->npassive);
   if (rc) return rc;
   AuxBlock<R> a;
   for (int k = 0; k < 3; k++) {
@@ -602,6 +626,7 @@ int aux_setup(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
   }
   a.f = fieldset_of<R>(b);
   a.pressure = (R*)b->pressure;
+  for (int k = 0; k < b->npassive; k++) a.pass[k] = (R*)b->passive[k];
   cudaError_t e = cudaMemcpyAsync(S.d_aux, &a, sizeof(a), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "aux upload");
   return MHD_OK;
@@ -901,6 +926,10 @@ extern "C" int mhdvlct_block_step_noalloc(mhdvlct_handle* h, const MhdBlockView*
   if (!h) return MHD_ERR_INVALID;
   int rc = check_view(h, b);
   if (rc) return rc;
+  if (b->npassive > 0)
+    return fail(h, MHD_ERR_INVALID,
+                "mhdvlct_block_step_noalloc does not advect passive scalars "
+                "(use mhdvlct_block_step)");
   if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
   cudaStream_t st = (cudaStream_t)stream;
   return b->dtype == MHD_DTYPE_F64 ? block_step_noalloc_t<double>(h, b, dt, st)

@@ -21,6 +21,7 @@ struct mhdvlct_handle {
   // plain-path scratch, reused while the block geometry and dtype repeat
   int cache_dtype = -1;
   int cache_m[3] = {0, 0, 0};
+  int cache_np = 0;            // passive-scalar scratch fields in the cache
   void* scratch = nullptr;     // one device allocation
   size_t scratch_bytes = 0;
   int tile = 0;                // tile extent used by the plain path

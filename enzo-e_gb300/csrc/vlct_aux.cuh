@@ -13,6 +13,7 @@ template <class R> struct AuxBlock {
   double cw[3];
   FieldSet<R> f;     // fields (cell + face)
   R* pressure;       // optional [w] pressure field
+  R* pass[4] = {nullptr, nullptr, nullptr, nullptr};  // passive scalars
 };
 
 // ---------------------------------------------------------------------------
@@ -167,12 +168,14 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
   const AuxBlock<R>& B = blocks[b];
   const int n[3] = {B.m[0] - 2 * g, B.m[1] - 2 * g, B.m[2] - 2 * g};
   for (int fs = 0; fs < nfield_slots; fs++) {
-    // slots 0..8 cell fields, 9..11 face fields, 12 the pressure field
-    // (Cello refreshes every field, EnzoMethodMHDVlct.cpp:146-151)
+    // slots 0..8 cell fields, 9..11 face fields, 12 the pressure field,
+    // 13..16 passive scalars (Cello refreshes every field,
+    // EnzoMethodMHDVlct.cpp:146-151)
     auto slot_ptr = [&](const AuxBlock<R>& X) -> R* {
       if (fs < NCELL) return X.f.c[fs];
       if (fs < NCELL + 3) return X.f.f[fs - NCELL];
-      return X.pressure;
+      if (fs == NCELL + 3) return X.pressure;
+      return X.pass[fs - NCELL - 4];
     };
     R* dst = slot_ptr(B);
     if (!dst) continue;

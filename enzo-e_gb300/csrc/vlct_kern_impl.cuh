@@ -14,8 +14,11 @@ template <class R, int SOLVER, int RECON, bool DE>
 cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
                       const StageInfo& info, const PhysParams& phys, int grid,
                       cudaStream_t st) {
-  const size_t smem = stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty);
-  auto k = stage_kernel<R, SOLVER, RECON, DE>;
+  const bool extra = info.fc != nullptr || info.gravity != 0 || info.npass > 0;
+  const size_t smem =
+      stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty, extra ? info.npass : 0);
+  auto k = extra ? stage_kernel<R, SOLVER, RECON, DE, true>
+                 : stage_kernel<R, SOLVER, RECON, DE, false>;
   cudaError_t e = cudaFuncSetAttribute(
       k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -121,7 +124,7 @@ cudaError_t launch_timestep<VLCT_REAL>(bool mhd, bool de,
 template <>
 cudaError_t launch_refresh<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, const int* nbr,
                                       int nb, int g, int cpb, cudaStream_t st) {
-  refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 4, cpb);
+  refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 8, cpb);
   return cudaGetLastError();
 }
 

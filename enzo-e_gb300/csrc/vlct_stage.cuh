@@ -78,8 +78,9 @@ struct SmemLayout {
   int HP, HQ;   // halo grid pitch / rows (tile + 1 cell each side)
   int G;        // HP * HQ
   int o_prim, o_xf, o_yf, o_zf, o_ec, o_ex, o_ey, o_ez, o_bx, o_by, o_bz;
+  int o_pprim, o_pf;  // passive scalars: specific-form ring, face fluxes
   int total;    // in elements of R
-  __host__ __device__ void init(int tx, int ty, int rp, int nring, int nf) {
+  __host__ __device__ void init(int tx, int ty, int rp, int nring, int nf, int np = 0) {
     PP = tx + 2 + 2 * rp;
     QP = ty + 2 + 2 * rp;
     HP = tx + 2;
@@ -97,15 +98,17 @@ struct SmemLayout {
     o_bx = o; o += G;
     o_by = o; o += G;
     o_bz = o; o += 2 * G;
+    o_pprim = o; o += nring * np * PP * QP;
+    o_pf = o; o += 3 * 2 * np * G;  // [dir][slot][scalar]
     total = o;
   }
 };
 
 template <class R, int SOLVER, int RECON, bool DE>
-size_t stage_smem_bytes(int tx, int ty) {
+size_t stage_smem_bytes(int tx, int ty, int np = 0) {
   using C = StageCfg<R, SOLVER, RECON, DE>;
   SmemLayout L;
-  L.init(tx, ty, C::RP, C::NRING, C::NF);
+  L.init(tx, ty, C::RP, C::NRING, C::NF, np);
   return (size_t)L.total * sizeof(R);
 }
 
@@ -135,7 +138,10 @@ inline int stage_max_threads(int recon) {
                                     : StageBounds<R, RECON_PLM_ATHENA>::threads;
 }
 
-template <class R, int SOLVER, int RECON, bool DE>
+// EXTRA: the instantiation that can also add the gravity source and store
+// the boundary fluxes for flux correction; the default one compiles both out
+// (their run-time checks alone cost ~4% of a stage).
+template <class R, int SOLVER, int RECON, bool DE, bool EXTRA>
 __global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
                                   StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
@@ -147,7 +153,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
   SmemLayout Ls;
-  Ls.init(info.tx, info.ty, RP, NRING, NF);
+  // passive scalars exist only in the EXTRA instantiation
+  const int NP = EXTRA ? info.npass : 0;
+  Ls.init(info.tx, info.ty, RP, NRING, NF, NP);
   const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;
   const int PQ = PP * QP;
   R* s_prim = sm + Ls.o_prim;
@@ -247,6 +255,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           w[(Q_BX + 2) * PQ] = bz;
         }
         w[Q_P * PQ] = p_out;
+        // passive scalars in specific form (EnzoPhysicsFluidProps.cpp:120-133)
+        for (int k = 0; k < NP; k++)
+          sm[Ls.o_pprim + (slot * NP + k) * PQ + poff(0, x, y)] = B.pass_cur[k][c] / rho;
         // cell-centred E = -v x B (EnzoBfieldMethodCT.cpp:267-292), on the
         // halo grid and inside [S, m - S)
         const int hi = x - hx0, hj = y - hy0;
@@ -373,11 +384,40 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           dst[S_EINT * G] = F.eflux;
           dst[S_VBAR * G] = F.vbar;
         }
+        // passive scalars (EnzoRiemannUtils.hpp:224-314): reconstruct the
+        // specific scalar like the primitives (no floor), flux = upwind value
+        // times the density flux; stored beside the face's other fluxes
+        for (int k = 0; k < NP; k++) {
+          const R* w = sm + Ls.o_pprim + k * PQ;
+          const int st = NP * PQ;  // ring-slot stride of the passive planes
+          auto at = [&](int o) { return w[(o / (NQ * PQ)) * st + (o % (NQ * PQ))]; };
+          R lv, rv;
+          if (RECON == RECON_NN) {
+            lv = at(off[1]);
+            rv = at(off[2]);
+          } else {
+            const R a = at(off[0]), b0 = at(off[1]), b1 = at(off[2]), c = at(off[3]);
+            R dl, dr;
+            if (RECON == RECON_PLM) {
+              dl = limiter_enzo_rk(a, b0, b1, theta);
+              dr = limiter_enzo_rk(b0, b1, c, theta);
+            } else {
+              dl = limiter_athena(a, b0, b1);
+              dr = limiter_athena(b0, b1, c);
+            }
+            lv = b0 + dl * R(0.5);
+            rv = b1 - dr * R(0.5);
+          }
+          const R df = F.f[L_RHO];
+          const R upwind = ((df > R(0)) ? R(1) : R(0)) * lv + ((df <= R(0)) ? R(1) : R(0)) * rv;
+          const int pslot = (d == 2) ? (t & 1) : (pl & 1);
+          sm[Ls.o_pf + ((d * 2 + pslot) * NP + k) * G + r] = upwind * df;
+        }
         // store_fluxes_for_corrections (EnzoMethodMHDVlct.cpp:250-330): the
         // final stage writes dt/dx times the flux through the block's active
         // boundary faces.  Every face is written by exactly one tile: the
         // tile (and z-chunk) that owns the cells on its high side.
-        if (info.fc != nullptr && info.final_stage) {
+        if (EXTRA && info.fc != nullptr && info.final_stage) {
           const FluxOut<R>* fo = static_cast<const FluxOut<R>*>(info.fc);
           const int gg = fo->g;
           const int fpos = d == 0 ? x : (d == 1 ? y : t);
@@ -593,7 +633,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           // gravity source on the full-dt stage (EnzoSourceGravity.cpp:17-69,
           // EnzoMHDIntegratorStageCommands.cpp:267-297): start-of-step
           // density and velocity
-          if (info.gravity) {
+          if (EXTRA && info.gravity) {
             const R dt = s_dt;
             const R rho0 = B.base.c[F_RHO][c];
             const R ax = B.accel[0][c], ay = B.accel[1][c], az = B.accel[2][c];
@@ -623,6 +663,19 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           B.out.c[F_VZ][c] = vz;
           B.out.c[F_ETOT][c] = etot;
           if (DE) B.out.c[F_EINT][c] = eint;
+          // update_passive_scalars_ (EnzoIntegrationQuanUpdate.cpp:242-270):
+          // conserved = start-of-step + dU
+          for (int k = 0; k < NP; k++) {
+            const R* fx = sm + Ls.o_pf + ((0 * 2 + (t & 1)) * NP + k) * G;
+            const R* fy = sm + Ls.o_pf + ((1 * 2 + (t & 1)) * NP + k) * G;
+            const R* fzp = sm + Ls.o_pf + ((2 * 2 + (t & 1)) * NP + k) * G;
+            const R* fzm = sm + Ls.o_pf + ((2 * 2 + ((t - 1) & 1)) * NP + k) * G;
+            R a = R(0.0);
+            a -= dtdx[0] * (fx[r] - fx[r - 1]);
+            a -= dtdx[1] * (fy[r] - fy[r - HP]);
+            a -= dtdx[2] * (fzp[r] - fzm[r]);
+            B.pass_out[k][c] = B.pass_base[k][c] + a;
+          }
         }
       }
       __syncthreads();

@@ -25,6 +25,11 @@ template <class R> struct StageBlock {
   FieldSet<R> base;      // start-of-step state (U^n, face B^n)
   FieldSet<R> out;       // where the stage writes (out.f = new face B)
   const R* accel[3] = {nullptr, nullptr, nullptr};  // gravity source fields
+  // passive scalars (conserved form): current-stage input, start of step,
+  // output; the first StageInfo::npass entries are used
+  const R* pass_cur[4] = {nullptr, nullptr, nullptr, nullptr};
+  const R* pass_base[4] = {nullptr, nullptr, nullptr, nullptr};
+  R* pass_out[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 // One unit of work: a column tile [xa, xb) x [ya, yb) of one block, whose
@@ -54,6 +59,7 @@ struct StageInfo {
                     // grid pulling tiles dynamically; null = static grid stride
   int threads;      // CTA size (256 or 512); 0 = 256
   int gravity = 0;           // 1: add the gravity source (the blocks' accel)
+  int npass = 0;             // passive scalars advected (0..4)
   const void* fc = nullptr;  // FluxOut<R> (device) on the final stage when the
                              // boundary fluxes are stored; null otherwise
 };

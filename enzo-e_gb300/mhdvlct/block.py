@@ -30,7 +30,7 @@ class Block:
 
     def __init__(self, n, ghost=3, cell_width=(1.0, 1.0, 1.0), mhd=True,
                  dual_energy=False, dtype=torch.float64, device="cuda",
-                 gravity=False):
+                 gravity=False, npassive=0):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
         self.n = (int(nx), int(ny), int(nz))
         self.ghost = int(ghost)
@@ -49,6 +49,8 @@ class Block:
             keys.append("internal_energy")
         if gravity:
             keys += ["acceleration_x", "acceleration_y", "acceleration_z"]
+        self.npassive = int(npassive)
+        keys += [f"passive_{k}" for k in range(self.npassive)]
         if mhd:
             keys += ["bfield_x", "bfield_y", "bfield_z"]
         self.fields = {k: torch.zeros(shp, dtype=dtype, device=device)
@@ -85,6 +87,9 @@ class Block:
         v.pressure = p("pressure")
         for a, k in enumerate(("acceleration_x", "acceleration_y", "acceleration_z")):
             v.acceleration[a] = p(k)
+        for k in range(self.npassive):
+            v.passive[k] = p(f"passive_{k}")
+        v.npassive = self.npassive
         return v
 
     # host <-> device helpers (tests, IC upload)

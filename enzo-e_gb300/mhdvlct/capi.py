@@ -77,7 +77,9 @@ class MhdBlockView(ctypes.Structure):
                 ("bfield", ctypes.c_void_p * 3),
                 ("bfieldi", ctypes.c_void_p * 3),
                 ("pressure", ctypes.c_void_p),
-                ("acceleration", ctypes.c_void_p * 3)]
+                ("acceleration", ctypes.c_void_p * 3),
+                ("passive", ctypes.c_void_p * 4),
+                ("npassive", ctypes.c_int)]
 
 
 class MhdServeRequest(ctypes.Structure):

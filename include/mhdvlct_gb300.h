@@ -113,6 +113,10 @@ typedef struct MhdBlockView {
                            * (EnzoSourceGravity.cpp:17-69, applied on the
                            * full-dt stage of the vl scheme); all three or
                            * none (NULL)                                      */
+  void* passive[4];       /* passively advected scalars in conserved form (a
+                           * density), e.g. Cello's "colour" fields
+                           * (EnzoIntegrationQuanUpdate.cpp:242-270)         */
+  int npassive;           /* number of passive scalars, 0..4                 */
 } MhdBlockView;
 
 /* EnzoMethodMHDVlct::compute (EnzoMethodMHDVlct.cpp:356-500): one VL+CT step

@@ -43,7 +43,8 @@ class OracleBlock(ctypes.Structure):
                 ("dy", ctypes.c_double), ("dz", ctypes.c_double)] + [
                     (n, _P) for n in ("rho", "vx", "vy", "vz", "etot", "eint",
                                       "bx", "by", "bz", "bfx", "bfy", "bfz",
-                                      "pressure", "ax", "ay", "az")]
+                                      "pressure", "ax", "ay", "az")] + [
+                    ("passive", _P * 4), ("npassive", ctypes.c_int)]
 
 
 def build(force: bool = False) -> str:
@@ -128,7 +129,7 @@ class Block:
     """One ghosted block held as float64 numpy arrays in Cello's layout."""
 
     def __init__(self, n, g=3, widths=(1.0, 1.0, 1.0), mhd=True,
-                 dual_energy=False, gravity=False):
+                 dual_energy=False, gravity=False, npassive=0):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else n
         self.n = (nx, ny, nz)
         self.g = g
@@ -146,6 +147,9 @@ class Block:
         if gravity:
             for k in ("ax", "ay", "az"):
                 self.f[k] = np.zeros(shp)
+        self.npassive = npassive
+        for k in range(npassive):
+            self.f[f"pass{k}"] = np.zeros(shp)
         if mhd:
             for k in ("bx", "by", "bz"):
                 self.f[k] = np.zeros(shp)
@@ -168,11 +172,16 @@ class Block:
             return a.ctypes.data_as(_P)
         nx, ny, nz = self.n
         dx, dy, dz = self.widths
-        return OracleBlock(nx, ny, nz, self.g, dx, dy, dz,
-                           *[p(k) for k in ("rho", "vx", "vy", "vz", "etot",
-                                            "eint", "bx", "by", "bz", "bfx",
-                                            "bfy", "bfz", "pressure", "ax",
-                                            "ay", "az")])
+        ob = OracleBlock(nx, ny, nz, self.g, dx, dy, dz,
+                         *[p(k) for k in ("rho", "vx", "vy", "vz", "etot",
+                                          "eint", "bx", "by", "bz", "bfx",
+                                          "bfy", "bfz", "pressure", "ax",
+                                          "ay", "az")])
+        npass = getattr(self, "npassive", 0)
+        for k in range(npass):
+            ob.passive[k] = p(f"pass{k}")
+        ob.npassive = npass
+        return ob
 
 
 def step(prm: OracleParams, b: Block, dt: float, ref: bool = False) -> None:

@@ -95,6 +95,8 @@ struct Views {
     put("acceleration_x", b->ax, 0, 0, 0);
     put("acceleration_y", b->ay, 0, 0, 0);
     put("acceleration_z", b->az, 0, 0, 0);
+    static const char* pnames[4] = {"pass0", "pass1", "pass2", "pass3"};
+    for (int k = 0; k < b->npassive && k < 4; k++) put(pnames[k], b->passive[k], 0, 0, 0);
   }
   EnzoEFltArrayMap map(const str_vec_t& keys) {
     std::vector<EFlt3DArray> arrs;
@@ -196,16 +198,24 @@ static int ref_step_impl(const OracleParams* p, OracleBlock* b, double dt,
     block.CellWidth[1] = b->dy;
     block.CellWidth[2] = b->dz;
 
-    const str_vec_t passive_list;
-    const str_vec_t integ_keys = s.integ->integration_quantity_keys();
-    const str_vec_t prim_keys = s.integ->primitive_quantity_keys();
+    // passive scalars (the lazy passive list of EnzoMethodMHDVlct::compute,
+    // :366) travel in every map after the integration quantities
+    str_vec_t passive_list;
+    for (int k = 0; k < b->npassive && k < 4; k++)
+      passive_list.push_back("pass" + std::to_string(k));
+    auto with_passive = [&](str_vec_t keys) {
+      keys.insert(keys.end(), passive_list.begin(), passive_list.end());
+      return keys;
+    };
+    const str_vec_t integ_keys = with_passive(s.integ->integration_quantity_keys());
+    const str_vec_t prim_keys = with_passive(s.integ->primitive_quantity_keys());
     EnzoEFltArrayMap external = views.map(integ_keys);
     const std::array<int, 3> shape = {external.array_shape(0),
                                       external.array_shape(1),
                                       external.array_shape(2)};
     const bool de = p->dual_energy != 0;
-    Scratch scratch(shape, integ_keys, prim_keys, s.integ->dUcons_map_keys(),
-                    de);
+    Scratch scratch(shape, integ_keys, prim_keys,
+                    with_passive(s.integ->dUcons_map_keys()), de);
     std::array<EnzoEFltArrayMap, 3> flux_maps = {
         scratch.xflux_map, scratch.yflux_map, scratch.zflux_map};
     // get_accel_map_ (EnzoMethodMHDVlct.cpp:219-233): empty without the

@@ -541,9 +541,13 @@ void hllc(double g, const double* wl, const double* wr, double* flux,
 /* ------------------------------------------------------------------------ */
 /* Block views                                                              */
 /* ------------------------------------------------------------------------ */
+constexpr int NPASS = 4;  // passive scalars supported
+
 struct Integ {  // views of the integration quantities (+ cell-centred B)
   V3 rho, vx, vy, vz, etot, eint;
   V3 b[3];
+  V3 pass[NPASS];  // passive scalars, conserved form
+  int np = 0;
   V3 v(int d) const { return d == 0 ? vx : (d == 1 ? vy : vz); }
 };
 
@@ -558,6 +562,8 @@ struct Scratch {
   A3 edge_e[3];
   A3 temp_face[3];
   A3 t_rho, t_vx, t_vy, t_vz, t_etot, t_eint, t_b[3];
+  // passive scalars: specific form, reconstructions, fluxes, dU, half step
+  A3 pprim[NPASS], pwl[NPASS], pwr[NPASS], pflux[3][NPASS], pdU[NPASS], t_pass[NPASS];
 };
 
 // Primitive quantities of one stage
@@ -596,6 +602,10 @@ void primitive_from_integration(const Ctx& c, const Integ& u, Scratch& sc,
     }
   });
   pressure_from_integration(c, u, sc.prim[Q_P].w, s);
+  // passive scalars from conserved to specific form
+  // (EnzoPhysicsFluidProps.cpp:120-133)
+  for (int k = 0; k < u.np; k++)
+    box(lo, hi, [&](const int* i) { sc.pprim[k].w.c(i) = u.pass[k].c(i) / u.rho.c(i); });
 }
 
 inline bool key_active(const Ctx& c, int q) {
@@ -604,10 +614,13 @@ inline bool key_active(const Ctx& c, int q) {
 
 // Reconstruction along dim (toolkit/EnzoReconstructorNN.cpp:14-49,
 // toolkit/EnzoReconstructorPLM.hpp:167-345).  wl/wr index f <-> face f+1/2.
-void reconstruct(const Ctx& c, Scratch& sc, int dim, int s, int recon) {
-  for (int q = 0; q < NQ; q++) {
-    if (!key_active(c, q)) continue;
-    V3 w = sc.prim[q].w, wl = sc.wl[q].w, wr = sc.wr[q].w;
+void reconstruct(const Ctx& c, Scratch& sc, int dim, int s, int recon, int np) {
+  for (int qq = 0; qq < NQ + np; qq++) {
+    const int q = qq < NQ ? qq : -1;  // -1: passive scalar qq - NQ (no floor)
+    if (q >= 0 && !key_active(c, q)) continue;
+    V3 w = q >= 0 ? sc.prim[q].w : sc.pprim[qq - NQ].w;
+    V3 wl = q >= 0 ? sc.wl[q].w : sc.pwl[qq - NQ].w;
+    V3 wr = q >= 0 ? sc.wr[q].w : sc.pwr[qq - NQ].w;
     int lo[3] = {s, s, s}, hi[3] = {c.m[0] - s, c.m[1] - s, c.m[2] - s};
     if (recon == ORC_NN) {
       hi[dim] -= 1;
@@ -687,11 +700,26 @@ void riemann(const Ctx& c, Scratch& sc, int dim, int S) {
     sc.vbar[dim].w.c(i) = vb;
   });
 }
+// solve_passive_advection (EnzoRiemannUtils.hpp:224-314): upwind specific
+// scalar times the density flux
+void passive_fluxes(const Ctx& c, Scratch& sc, int dim, int S, int np) {
+  int lo[3] = {S, S, S}, hi[3] = {c.m[0] - S, c.m[1] - S, c.m[2] - S};
+  hi[dim] -= 1;
+  const V3 dens_flux = sc.flux[dim][Q_RHO].w;
+  for (int k = 0; k < np; k++) {
+    const V3 wl = sc.pwl[k].w, wr = sc.pwr[k].w, F = sc.pflux[dim][k].w;
+    box(lo, hi, [&](const int* i) {
+      const double df = dens_flux.c(i);
+      const double upwind = (df > 0) * wl.c(i) + (df <= 0) * wr.c(i);
+      F.c(i) = upwind * df;
+    });
+  }
+}
 
 // EnzoIntegrationQuanUpdate::accumulate_flux_component (:105-147) and
 // EnzoSourceInternalEnergy::calculate_source (:16-92)
 void accumulate(const Ctx& c, Scratch& sc, int dim, double dt,
-                double cell_width, int S) {
+                double cell_width, int S, int np) {
   const double dtdx_i = dt / cell_width;
   int lo[3] = {S, S, S}, hi[3] = {c.m[0] - S, c.m[1] - S, c.m[2] - S};
   lo[dim] += 1;
@@ -700,6 +728,14 @@ void accumulate(const Ctx& c, Scratch& sc, int dim, double dt,
   const int fkey[5] = {Q_RHO, Q_VX, Q_VY, Q_VZ, Q_P};
   for (int k = 0; k < 5; k++) {
     V3 dU = sc.dU[k].w, F = sc.flux[dim][fkey[k]].w;
+    box(lo, hi, [&](const int* i) {
+      int im[3] = {i[0], i[1], i[2]};
+      im[dim] -= 1;
+      dU.c(i) -= dtdx_i * (F.c(i) - F.c(im));
+    });
+  }
+  for (int k = 0; k < np; k++) {
+    V3 dU = sc.pdU[k].w, F = sc.pflux[dim][k].w;
     box(lo, hi, [&](const int* i) {
       int im[3] = {i[0], i[1], i[2]};
       im[dim] -= 1;
@@ -892,6 +928,9 @@ void update_quantities(const Ctx& c, const Integ& begin, Scratch& sc,
     }
   });
   energy_floor_sync(c, out, S + 1);
+  // update_passive_scalars_ (EnzoIntegrationQuanUpdate.cpp:242-270)
+  for (int k = 0; k < begin.np; k++)
+    box(lo, hi, [&](const int* i) { out.pass[k].c(i) = begin.pass[k].c(i) + sc.pdU[k].w.c(i); });
 }
 
 int staling_total(int recon) { return recon == ORC_NN ? 1 : 2; }
@@ -926,13 +965,16 @@ void compute_update_stage(const Ctx& c, const Integ& begin, const Integ& cur,
                           const double* cw, int recon, double cur_dt,
                           int stale, bool full_timestep) {
   for (int k = 0; k < 6; k++) std::fill(sc.dU[k].v.begin(), sc.dU[k].v.end(), 0.0);
+  const int np = cur.np;
+  for (int k = 0; k < np; k++) std::fill(sc.pdU[k].v.begin(), sc.pdU[k].v.end(), 0.0);
   primitive_from_integration(c, cur, sc, stale);
   for (int dim = 0; dim < 3; dim++) {
-    reconstruct(c, sc, dim, stale, recon);
+    reconstruct(c, sc, dim, stale, recon, np);
     int cs = stale + staling_immediate(recon);
     if (c.mhd) correct_bfield(c, sc, face_cur, dim, cs);
     riemann(c, sc, dim, cs);
-    accumulate(c, sc, dim, cur_dt, cw[dim], cs);
+    passive_fluxes(c, sc, dim, cs, np);
+    accumulate(c, sc, dim, cur_dt, cw[dim], cs, np);
     if (c.mhd) identify_upwind(c, sc, dim, cs);
   }
   stale += staling_immediate(recon);
@@ -964,6 +1006,8 @@ Integ integ_of(const OracleBlock* b, const int* m) {
   u.b[0] = view(b->bx, m[0], m[1], m[2]);
   u.b[1] = view(b->by, m[0], m[1], m[2]);
   u.b[2] = view(b->bz, m[0], m[1], m[2]);
+  u.np = std::max(0, std::min(b->npassive, NPASS));
+  for (int k = 0; k < u.np; k++) u.pass[k] = view(b->passive[k], m[0], m[1], m[2]);
   return u;
 }
 
@@ -1093,6 +1137,17 @@ static int step_impl(const OracleParams* p, OracleBlock* b, double dt,
   tmp.rho = sc.t_rho.w; tmp.vx = sc.t_vx.w; tmp.vy = sc.t_vy.w;
   tmp.vz = sc.t_vz.w; tmp.etot = sc.t_etot.w; tmp.eint = sc.t_eint.w;
   for (int d = 0; d < 3; d++) tmp.b[d] = sc.t_b[d].w;
+  tmp.np = ext.np;
+  for (int k = 0; k < ext.np; k++) {
+    sc.pprim[k].alloc(m[0], m[1], m[2]);
+    sc.pwl[k].alloc(m[0], m[1], m[2]);
+    sc.pwr[k].alloc(m[0], m[1], m[2]);
+    sc.pdU[k].alloc(m[0], m[1], m[2]);
+    sc.t_pass[k].alloc(m[0], m[1], m[2]);
+    tmp.pass[k] = sc.t_pass[k].w;
+    for (int d = 0; d < 3; d++)
+      sc.pflux[d][k].alloc(m[0] - (d == 0), m[1] - (d == 1), m[2] - (d == 2));
+  }
 
   V3 face[3];
   if (c.mhd) {

@@ -43,6 +43,8 @@ typedef struct {
   double *bfx, *bfy, *bfz;                       /* face-centred B (MHD)      */
   double *pressure;                              /* [w] scratch field         */
   double *ax, *ay, *az;  /* acceleration_x/y/z (gravity source), or NULL     */
+  double *passive[4];    /* passively advected scalars, conserved form (a     */
+  int npassive;          /* density), npassive <= 4                           */
 } OracleBlock;
 
 /* The step with store_fluxes_for_corrections (hydro only): after the final

@@ -57,7 +57,7 @@ def test_fp64_gravity_step_bit_exact(solver, recon, de, scheme):
 
 @pytest.mark.parametrize("solver,recon,de,scheme", CASES[:2])
 def test_fp32_gravity_step_close(solver, recon, de, scheme):
-    meth, blk, ob, prm = _pair(solver, recon, de, scheme, torch.float32, n=10)
+    meth, blk, ob, prm = _pair(solver, recon, de, scheme, torch.float32, n=(10, 10, 10))
     dt = O.timestep(prm, ob)
     meth.timestep(blk)
     O.step(prm, ob, dt)
