@@ -249,7 +249,8 @@ cudaError_t launch_timestep_b(mhdvlct_batch* b, int global_min, cudaStream_t st)
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
-  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 2048, 64));
+  // about two cells per thread: enough warps in flight to cover the loads
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 512, 256));
   return launch_timestep<R>(b->h->mhd != 0, b->h->de != 0,
                             (const AuxBlock<R>*)b->d_aux[b->parity], b->nblocks, cpb,
                             b->h->phys, b->d_smax, b->h->params.courant, global_min,
@@ -261,9 +262,11 @@ cudaError_t launch_refresh_b(mhdvlct_batch* b, cudaStream_t st) {
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
-  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 4096, 32));
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 1024, 128));
+  int max_m = 0;
+  for (auto& o : b->off) max_m = std::max(max_m, std::max(o.m[0], std::max(o.m[1], o.m[2])));
   return launch_refresh<R>((const AuxBlock<R>*)b->d_aux[b->parity], b->d_nbr,
-                           b->nblocks, b->g, cpb, st);
+                           b->nblocks, b->g, cpb, max_m, st);
 }
 
 template <class R>

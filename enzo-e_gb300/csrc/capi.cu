@@ -656,7 +656,9 @@ int fill_ghosts_t(mhdvlct_handle* h, const MhdBlockView* b, cudaStream_t st) {
   PlainScratch<R> S;
   int rc = aux_setup<R>(h, b, S, st);
   if (rc) return rc;
-  cudaError_t e = launch_refresh<R>(S.d_aux, S.d_nbr, 1, b->ghost[0], 64, st);
+  const int g = b->ghost[0];
+  const int max_m = std::max(b->n[0], std::max(b->n[1], b->n[2])) + 2 * g;
+  cudaError_t e = launch_refresh<R>(S.d_aux, S.d_nbr, 1, g, 64, max_m, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "refresh launch");
   return MHD_OK;
 }

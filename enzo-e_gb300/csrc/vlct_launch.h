@@ -32,9 +32,11 @@ cudaError_t launch_timestep(bool mhd, bool de, const AuxBlock<R>* d_blocks,
                             double courant, int global_min, double* d_dt,
                             double* d_dt_min, cudaStream_t st);
 
+// max_m: the largest ghosted extent of any block (selects the multiply-high
+// shell decode when it is exact for every block)
 template <class R>
 cudaError_t launch_refresh(const AuxBlock<R>* d_blocks, const int* d_nbr,
-                           int nblocks, int g, int chunks_per_block,
+                           int nblocks, int g, int chunks_per_block, int max_m,
                            cudaStream_t st);
 
 template <class R>
