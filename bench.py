@@ -730,27 +730,52 @@ def main():
     # ------------------------------------------------------ e2e (host data)
     e2e = None
     if not a.no_e2e:
+        # the host keeps the state (every block's cells and its current
+        # face-B buffer, one or two contiguous segments); each step copies it
+        # in, runs one cycle through the C ABI and copies the new state back
         rt = _cudart()
+        segp = (ctypes.c_void_p * 2)()
+        segb = (ctypes.c_size_t * 2)()
+        nseg = ctypes.c_int()
+
+        def segments():
+            capi.check(L.mhdvlct_batch_state_segments(h32, segp, segb, 2,
+                                                      ctypes.byref(nseg)), meth.handle)
+            return [(segp[i], segb[i]) for i in range(nseg.value)]
+
+        total = sum(n for _, n in segments())
         dptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
         capi.check(L.mhdvlct_batch_state_region(h32, ctypes.byref(dptr),
                                                 ctypes.byref(nbytes)))
         host = torch.empty(nbytes.value, dtype=torch.uint8, pin_memory=True)
-        assert rt.cudaMemcpy(host.data_ptr(), dptr.value, nbytes.value, 2) == 0
+
+        def copy(to_device):
+            off = 0
+            for p_, n_ in segments():
+                if to_device:
+                    assert rt.cudaMemcpyAsync(p_, host.data_ptr() + off, n_, 1, sp) == 0
+                else:
+                    assert rt.cudaMemcpyAsync(host.data_ptr() + off, p_, n_, 2, sp) == 0
+                off += n_
+            return off
+
+        copy(False)
         e2e_steps = max(1, min(a.steps, 5))
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        h2d = d2h = 0
         e0.record(stream)
         for _ in range(e2e_steps):
-            assert rt.cudaMemcpyAsync(dptr.value, host.data_ptr(), nbytes.value, 1, sp) == 0
+            h2d += copy(True)
             capi.check(L.mhdvlct_batch_run(h32, 1, 0, None, sp), meth.handle, "e2e")
-            assert rt.cudaMemcpyAsync(host.data_ptr(), dptr.value, nbytes.value, 2, sp) == 0
+            d2h += copy(False)
         e1.record(stream)
         torch.cuda.synchronize()
         e_ms = e0.elapsed_time(e1)
         e2e = {"value": world * zones * e2e_steps / (e_ms / 1e3),
-               "unit": "zone-updates/s", "h2d_bytes_per_step": int(nbytes.value),
-               "d2h_bytes_per_step": int(nbytes.value), "steps": e2e_steps}
+               "unit": "zone-updates/s", "h2d_bytes_per_step": int(h2d // e2e_steps),
+               "d2h_bytes_per_step": int(d2h // e2e_steps), "steps": e2e_steps}
     L.mhdvlct_batch_destroy(h32)
 
     # ------------------------------------------- FP64: batched and plain path

@@ -49,6 +49,9 @@ struct mhdvlct_batch {
   void* pool = nullptr;
   size_t pool_bytes = 0;
   size_t state_elems = 0;  // leading part of the pool holding the state
+  size_t cells_elems = 0;  // cell fields of every block: [0, cells_elems)
+  size_t fa_end = 0;       // face buffer A of every block: [cells_elems, fa_end),
+                           // buffer B: [fa_end, state_elems)
   // element offsets (in units of the real type) of every array of block i
   struct Off {
     size_t ext[NCELL], tmp[NCELL], fa[3], fb[3], tf[3], pres;
@@ -249,8 +252,7 @@ cudaError_t launch_timestep_b(mhdvlct_batch* b, int global_min, cudaStream_t st)
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
-  // about two cells per thread: enough warps in flight to cover the loads
-  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 512, 256));
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 2048, 64));
   return launch_timestep<R>(b->h->mhd != 0, b->h->de != 0,
                             (const AuxBlock<R>*)b->d_aux[b->parity], b->nblocks, cpb,
                             b->h->phys, b->d_smax, b->h->params.courant, global_min,
@@ -262,7 +264,7 @@ cudaError_t launch_refresh_b(mhdvlct_batch* b, cudaStream_t st) {
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
-  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 1024, 128));
+  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 4096, 32));
   int max_m = 0;
   for (auto& o : b->off) max_m = std::max(max_m, std::max(o.m[0], std::max(o.m[1], o.m[2])));
   return launch_refresh<R>((const AuxBlock<R>*)b->d_aux[b->parity], b->d_nbr,
@@ -328,17 +330,30 @@ extern "C" int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
         if (pass == 0) O.ext[k] = used ? take(M) : (size_t)-1;
         else O.tmp[k] = used ? take(M) : (size_t)-1;
       }
-      for (int d = 0; d < 3; d++) {
-        if (pass == 0) {
-          O.fa[d] = h->mhd ? take(F[d]) : (size_t)-1;
-          O.fb[d] = h->mhd ? take(F[d]) : (size_t)-1;
-        } else {
-          O.tf[d] = h->mhd ? take(F[d]) : (size_t)-1;
-        }
-      }
+      for (int d = 0; d < 3; d++)
+        if (pass == 1) O.tf[d] = h->mhd ? take(F[d]) : (size_t)-1;
       if (pass == 1) O.pres = take(M);
     }
-    if (pass == 0) b->state_elems = o;
+    if (pass == 0) {
+      // the face-B buffers after all cell fields, buffer A of every block
+      // then buffer B of every block: the current state (cells + the current
+      // buffer) is then at most two contiguous segments
+      b->cells_elems = o;
+      for (int buf = 0; buf < 2; buf++) {
+        for (int i = 0; i < nblocks; i++) {
+          auto& O = b->off[i];
+          const size_t F[3] = {(size_t)(O.m[0] + 1) * O.m[1] * O.m[2],
+                               (size_t)O.m[0] * (O.m[1] + 1) * O.m[2],
+                               (size_t)O.m[0] * O.m[1] * (O.m[2] + 1)};
+          for (int d = 0; d < 3; d++) {
+            const size_t at = h->mhd ? take(F[d]) : (size_t)-1;
+            (buf == 0 ? O.fa[d] : O.fb[d]) = at;
+          }
+        }
+        if (buf == 0) b->fa_end = o;
+      }
+      b->state_elems = o;
+    }
   }
   b->pool_bytes = o * esz;
   cudaError_t e = cudaMalloc(&b->pool, b->pool_bytes);
@@ -551,6 +566,26 @@ extern "C" int mhdvlct_batch_set_stage_tile(mhdvlct_batch* b, int stage, int til
   }
   b->threads[stage] = threads ? threads : 256;
   return build_descriptors_any(b, 0);
+}
+
+extern "C" int mhdvlct_batch_state_segments(mhdvlct_batch* b, void** dev_ptrs,
+                                            size_t* bytes, int max_segments,
+                                            int* nsegments) {
+  if (!b || !dev_ptrs || !bytes || !nsegments || max_segments < 2) return MHD_ERR_INVALID;
+  const size_t esz = b->dtype == MHD_DTYPE_F64 ? 8 : 4;
+  char* base = (char*)b->pool;
+  dev_ptrs[0] = base;
+  if (!b->h->mhd || b->parity == 0) {
+    // cells followed by the current face buffer A: one segment
+    bytes[0] = (b->h->mhd ? b->fa_end : b->cells_elems) * esz;
+    *nsegments = 1;
+  } else {
+    bytes[0] = b->cells_elems * esz;
+    dev_ptrs[1] = base + b->fa_end * esz;
+    bytes[1] = (b->state_elems - b->fa_end) * esz;
+    *nsegments = 2;
+  }
+  return MHD_OK;
 }
 
 extern "C" int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,

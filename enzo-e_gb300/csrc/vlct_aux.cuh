@@ -57,29 +57,40 @@ timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
   EnergyConsts<R> econ;
   econ.init(phys.gamma, phys.pressure_floor, DE ? phys.eta : 0.0);
   R s[3] = {R(0), R(0), R(0)};
+  // the block's field pointers in registers: the descriptor lives in global
+  // memory, and the stores below would otherwise force a reload per cell
+  const R* const f_rho = B.f.c[F_RHO];
+  const R* const f_vx = B.f.c[F_VX];
+  const R* const f_vy = B.f.c[F_VY];
+  const R* const f_vz = B.f.c[F_VZ];
+  const R* const f_bx = B.f.c[F_BX];
+  const R* const f_by = B.f.c[F_BY];
+  const R* const f_bz = B.f.c[F_BZ];
+  R* const f_etot = B.f.c[F_ETOT];
+  R* const f_eint = B.f.c[F_EINT];
+  R* const f_p = B.pressure;
   for (size_t c = (size_t)chunk * blockDim.x + threadIdx.x; c < ncell;
        c += (size_t)chunks_per_block * blockDim.x) {
-    const R rho = B.f.c[F_RHO][c];
-    const R vx = B.f.c[F_VX][c], vy = B.f.c[F_VY][c], vz = B.f.c[F_VZ][c];
+    const R rho = f_rho[c];
+    const R vx = f_vx[c], vy = f_vy[c], vz = f_vz[c];
     R bx = R(0), by = R(0), bz = R(0);
     if (MHD) {
-      bx = B.f.c[F_BX][c];
-      by = B.f.c[F_BY][c];
-      bz = B.f.c[F_BZ][c];
+      bx = f_bx[c];
+      by = f_by[c];
+      bz = f_bz[c];
     }
     R p;
     if (DE) {
       // apply_floor_to_energy_and_sync over the whole block (stale depth 0)
-      R etot = B.f.c[F_ETOT][c], eint = B.f.c[F_EINT][c];
+      R etot = f_etot[c], eint = f_eint[c];
       energy_floor_sync<MHD, true>(econ, rho, vx, vy, vz, bx, by, bz, etot, eint);
-      B.f.c[F_EINT][c] = eint;
-      B.f.c[F_ETOT][c] = etot;
+      f_eint[c] = eint;
+      f_etot[c] = etot;
       p = econ.gm1 * rho * eint;
     } else {
-      p = pressure_from_etot<R, MHD>(econ, rho, B.f.c[F_ETOT][c], vx, vy, vz, bx, by,
-                                     bz);
+      p = pressure_from_etot<R, MHD>(econ, rho, f_etot[c], vx, vy, vz, bx, by, bz);
     }
-    if (B.pressure) B.pressure[c] = p;
+    if (f_p) f_p[c] = p;
     R cf;
     if (MHD) {  // fast_magnetosonic_speed<0> (EnzoEOSIdeal.hpp:124-126)
       const R B2 = sqmag(bx, by, bz);

@@ -179,6 +179,10 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   const FastDiv divPP(Ls.PP), divHP(Ls.HP);
 
   __shared__ int s_next;
+  // the current tile's block descriptor, copied into shared memory once per
+  // tile: read from global memory, its field pointers would be reloaded after
+  // every global store (the compiler cannot rule out aliasing)
+  __shared__ __align__(16) unsigned long long s_blk_raw[(sizeof(StageBlock<R>) + 7) / 8];
   __shared__ R s_dtdx[3];
   __shared__ R s_dt;
   int it = blockIdx.x;
@@ -189,19 +193,26 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   }
   while (it < ntiles) {
     const StageTile tl = tiles[it];
-    const StageBlock<R>& B = blocks[tl.block];
-    const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
+    {
+      const unsigned long long* src =
+          reinterpret_cast<const unsigned long long*>(blocks + tl.block);
+      for (int w = tid; w < (int)((sizeof(StageBlock<R>) + 7) / 8); w += nthr)
+        s_blk_raw[w] = src[w];
+    }
+    const StageBlock<R>& B = *reinterpret_cast<const StageBlock<R>*>(s_blk_raw);
+    const StageBlock<R>& Bg = blocks[tl.block];
+    const int m0 = Bg.m[0], m1 = Bg.m[1], m2 = Bg.m[2];
     const int xa = tl.xa, xb = tl.xb, ya = tl.ya, yb = tl.yb;
     const int tx = xb - xa, ty = yb - ya;
     // dt / dx per axis, once per tile (FP64 divisions: one thread)
     if (tid == 0) {
-      const double dt = *B.dt * info.dt_factor;
-      s_dtdx[0] = R(dt / B.cw[0]);
-      s_dtdx[1] = R(dt / B.cw[1]);
-      s_dtdx[2] = R(dt / B.cw[2]);
+      const double dt = *Bg.dt * info.dt_factor;
+      s_dtdx[0] = R(dt / Bg.cw[0]);
+      s_dtdx[1] = R(dt / Bg.cw[1]);
+      s_dtdx[2] = R(dt / Bg.cw[2]);
       s_dt = R(dt);
     }
-    __syncthreads();
+    __syncthreads();  // also publishes the descriptor copy
     const R dtdx[3] = {s_dtdx[0], s_dtdx[1], s_dtdx[2]};
     // output window of centred B (and the z-march range)
     const int olo = info.final_stage ? S : S + 1;

@@ -237,6 +237,12 @@ int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,
  * Synchronises the stream.  (The reference computes such sums in its
  * analysis scripts; no Method counterpart.) */
 int mhdvlct_batch_diagnostics(mhdvlct_batch* b, double* out, void* stream);
+/* The current state only (every block's cell fields and its current face-B
+ * buffer), as one or two contiguous device segments: dev_ptrs[i] / bytes[i]
+ * for i < *nsegments (max_segments >= 2).  Valid until the next step; what a
+ * host that keeps the fields transfers each cycle. */
+int mhdvlct_batch_state_segments(mhdvlct_batch* b, void** dev_ptrs, size_t* bytes,
+                                 int max_segments, int* nsegments);
 /* Run `reps` cycles as individual launches with CUDA events between the
  * kernels; ms_out[0..4] = mean ms per cycle of the timestep reduction, the
  * ghost refresh, stage 1 (half dt), stage 2 (full dt) and the whole cycle. */

@@ -242,3 +242,41 @@ def test_diagnostics_totals_and_conservation(dtype):
     bmax = d1[7]
     divb_tol = 1e-12 if dtype == capi.MHD_DTYPE_F64 else 1e-5
     assert d1[6] * w[0] / bmax <= divb_tol
+
+
+def test_state_segments_cover_the_current_state():
+    """mhdvlct_batch_state_segments: the current state (every cell field and
+    the current face-B buffer of every block), one segment after an even
+    number of cycles and two after an odd one; every field a block view
+    points at lies inside them."""
+    meth = B.EnzoMethodMHDVlct()
+    sizes = [(8, 8, 8), (6, 10, 7)]
+    states, widths = [], []
+    for i, n in enumerate(sizes):
+        s, w = ic.smooth_block(n, 3, seed=300 + i)
+        states.append(s)
+        widths.append(w)
+    bt = Batch(meth, sizes, widths)
+    for i, s in enumerate(states):
+        bt.upload(i, s)
+    segp = (ctypes.c_void_p * 2)()
+    segb = (ctypes.c_size_t * 2)()
+    nseg = ctypes.c_int()
+    for cycles, expect in ((0, 1), (1, 2), (1, 1)):
+        if cycles:
+            capi.check(capi.lib().mhdvlct_batch_run(bt.h, cycles, 0, None, None))
+        capi.check(capi.lib().mhdvlct_batch_state_segments(bt.h, segp, segb, 2,
+                                                           ctypes.byref(nseg)))
+        assert nseg.value == expect
+        segs = [(segp[i], segb[i]) for i in range(nseg.value)]
+        want, narr = 0, 0
+        for i, n in enumerate(sizes):
+            for k, (p, shp) in bt.tensors(i).items():
+                if k == "pressure":
+                    continue
+                nbytes = int(np.prod(shp)) * 8
+                want += nbytes
+                narr += 1
+                assert any(a <= p and p + nbytes <= a + b for a, b in segs), (i, k)
+        # every array is padded to a 256-byte boundary
+        assert want <= sum(b for _, b in segs) < want + narr * 256
