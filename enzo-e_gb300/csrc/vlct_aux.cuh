@@ -59,16 +59,19 @@ timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
   R s[3] = {R(0), R(0), R(0)};
   // the block's field pointers in registers: the descriptor lives in global
   // memory, and the stores below would otherwise force a reload per cell
-  const R* const f_rho = B.f.c[F_RHO];
-  const R* const f_vx = B.f.c[F_VX];
-  const R* const f_vy = B.f.c[F_VY];
-  const R* const f_vz = B.f.c[F_VZ];
-  const R* const f_bx = B.f.c[F_BX];
-  const R* const f_by = B.f.c[F_BY];
-  const R* const f_bz = B.f.c[F_BZ];
-  R* const f_etot = B.f.c[F_ETOT];
-  R* const f_eint = B.f.c[F_EINT];
-  R* const f_p = B.pressure;
+  // (distinct arrays: restrict lets the loads of later cells move ahead of
+  // the stores of earlier ones)
+  const R* __restrict__ const f_rho = B.f.c[F_RHO];
+  const R* __restrict__ const f_vx = B.f.c[F_VX];
+  const R* __restrict__ const f_vy = B.f.c[F_VY];
+  const R* __restrict__ const f_vz = B.f.c[F_VZ];
+  const R* __restrict__ const f_bx = B.f.c[F_BX];
+  const R* __restrict__ const f_by = B.f.c[F_BY];
+  const R* __restrict__ const f_bz = B.f.c[F_BZ];
+  R* __restrict__ const f_etot = B.f.c[F_ETOT];
+  R* __restrict__ const f_eint = B.f.c[F_EINT];
+  R* __restrict__ const f_p = B.pressure;
+#pragma unroll 4
   for (size_t c = (size_t)chunk * blockDim.x + threadIdx.x; c < ncell;
        c += (size_t)chunks_per_block * blockDim.x) {
     const R rho = f_rho[c];
