@@ -103,13 +103,41 @@ TileChoice choice_for(const mhdvlct_batch* b, int i) {
   std::vector<int> key(b->dims.begin() + 3 * i, b->dims.begin() + 3 * i + 3);
   auto it = b->tune.find(key);
   TileChoice c;
-  if (it != b->tune.end()) c = it->second;
+  const bool tuned = it != b->tune.end();
+  if (tuned) c = it->second;
   const StagePlan sp = stage_plan(b->h);
   for (int s = 0; s < 2; s++)
     if (c.tile_x[s] <= 0 || c.tile_y[s] <= 0) {
       const int t = default_tile(b->dtype, b->h->solver, sp.recon[s], b->h->de);
       c.tile_x[s] = c.tile_y[s] = t;
     }
+  if (!tuned) {
+    // untuned default: when the batch has too few column tiles to fill the
+    // GPU (a few large blocks, e.g. one serving request), cut the columns
+    // into z-chunks so that a stage has about two waves of tiles
+    static int nsm = 0;
+    if (nsm == 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          nsm <= 0)
+        nsm = 1;
+    }
+    const int target = 4 * nsm;
+    for (int s = 0; s < 2; s++) {
+      long columns = 0;
+      for (int k = 0; k < b->nblocks; k++) {
+        const int mx = b->dims[3 * k] + 2 * b->g, my = b->dims[3 * k + 1] + 2 * b->g;
+        columns += (long)((mx + c.tile_x[s] - 1) / c.tile_x[s]) *
+                   ((my + c.tile_y[s] - 1) / c.tile_y[s]);
+      }
+      const int mz = b->dims[3 * i + 2] + 2 * b->g;
+      if (columns < target && mz > 24) {
+        const long chunks = (target + columns - 1) / columns;
+        c.zchunk[s] = std::max(8, (int)((mz + chunks - 1) / chunks));
+      }
+    }
+  }
   return c;
 }
 

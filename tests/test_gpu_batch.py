@@ -280,3 +280,26 @@ def test_state_segments_cover_the_current_state():
                 assert any(a <= p and p + nbytes <= a + b for a, b in segs), (i, k)
         # every array is padded to a 256-byte boundary
         assert want <= sum(b for _, b in segs) < want + narr * 256
+
+
+def test_zchunked_default_tiles_bit_exact():
+    """One large block alone: the default work decomposition cuts its columns
+    into z-chunks (too few column tiles to fill the GPU); the FP64 result is
+    still the oracle's bit for bit, after two cycles."""
+    meth = B.EnzoMethodMHDVlct()
+    n = (26, 20, 40)
+    s, w = ic.smooth_block(n, 3, seed=404)
+    bt = Batch(meth, [n], [w])
+    bt.upload(0, s)
+    capi.check(capi.lib().mhdvlct_batch_run(bt.h, 2, 0, None, None))
+    ob = oracle_block(s, n, 3, w)
+    prm = oracle_params(courant=meth.courant)
+    for _ in range(2):
+        dt = O.timestep(prm, ob)
+        O.fill_ghosts_periodic(ob)
+        O.step(prm, ob, dt)
+    got = bt.download(0)
+    g = 3
+    act = (slice(g, g + n[2]), slice(g, g + n[1]), slice(g, g + n[0]))
+    for k in KEYS[:8]:
+        assert np.array_equal(got[k][act], ob.f[ic.ORACLE_NAME[k]][act]), k
