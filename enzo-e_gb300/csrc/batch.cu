@@ -8,7 +8,11 @@
 // queue).  The face-centred B is double buffered: the last stage reads the
 // start-of-step faces and writes the other buffer, so no stage updates a
 // field in place that another CTA may still read.  The whole cycle is
-// captured once as a CUDA graph per face-buffer parity and replayed.
+// captured once as a CUDA graph per face-buffer parity and replayed.  The
+// pool holds every block's cell fields, then face buffer A of every block,
+// then buffer B, so the current state is at most two contiguous segments.
+// Tiles, z-chunks and CTA sizes come from the autotuner per block-size class
+// and stage (or a default that z-chunks a batch too small to fill the GPU).
 #include <algorithm>
 #include <chrono>
 #include <cmath>

@@ -1,5 +1,7 @@
 // capi.cu -- C ABI: parameters, handle and the per-block Method operations
-// (EnzoMethodMHDVlct::compute / ::timestep and the ghost refresh).
+// (EnzoMethodMHDVlct::compute / ::timestep and the ghost refresh), with the
+// optional gravity source, passive scalars and flux-correction output, and
+// the no-allocation variant of the step.
 #include <algorithm>
 #include <cctype>
 #include <cmath>

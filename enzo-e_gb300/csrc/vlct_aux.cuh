@@ -1,5 +1,6 @@
 // vlct_aux.cuh -- the kernels around the fused stages: the CFL timestep
-// reduction, the same-level ghost refresh gather and small copy helpers.
+// reduction, the same-level ghost refresh gather, the FP64 conserved-total /
+// div B diagnostics and small copy helpers.
 #pragma once
 #include "vlct_energy.cuh"
 #include "vlct_physics.cuh"

@@ -2,17 +2,17 @@
 // blocks, as a z-marching CUDA kernel.
 //
 // A CTA owns a column tile [xa, xb) x [ya, yb) of one block and marches up
-// the block's z range.  Everything between the global state read and the
-// stage's outputs stays in shared memory: the primitives of a ring of
-// z-planes, the x/y face fluxes of two planes, the z-face fluxes of two
-// faces, the cell-centred electric field, the edge EMFs and the new face B.
-// Per z-plane the CTA runs five phases separated by __syncthreads():
+// the block's z range (or one z-chunk of it).  Everything between the global
+// state read and the stage's outputs stays in shared memory: the primitives
+// and cell-centred E of a ring of z-planes, the x/y face fluxes of two
+// planes, the z-face fluxes of two faces, the edge EMFs and the new face B.
+// Per z-plane t the CTA runs four phases separated by __syncthreads():
 //
-//   A  load primitives of plane t+L (L = 1 for NN, 2 for PLM)
-//   B  Riemann solves: z-faces at t+1/2, x- and y-faces of plane t+1;
-//      cell-centred E of plane t+1
+//   B  Riemann solves: z-faces at t+1/2, x- and y-faces of plane t+1
 //   C  upwinded edge EMFs: E_x, E_y at t+1/2 and E_z of plane t
-//   D1 constrained-transport face updates: Bz at t+1/2, Bx / By of plane t
+//   D1 constrained-transport face updates (Bz at t+1/2, Bx / By of plane t),
+//      and the primitives + cell-centred E of plane t+1+L (L = 1 for NN, 2
+//      for PLM) loaded into the ring for the next plane
 //   D2 cell updates of plane t: centred B, flux divergence + dual-energy
 //      source, density floor, energy floor / dual-energy sync; store.
 //
@@ -24,7 +24,9 @@
 // them.  The FP64 instantiation is compiled with --fmad=false and matches the
 // reference bit for bit; in the FP32 instantiation the pressure recovery
 // (total minus kinetic minus magnetic energy) and the energy floor / sync run
-// in FP64.
+// in float-float (vlct_energy.cuh).  A second instantiation (EXTRA) also
+// adds the gravity source, advects passive scalars and stores the boundary
+// fluxes for flux correction; the default one compiles those out.
 #pragma once
 #include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
