@@ -119,14 +119,15 @@ TileChoice choice_for(const mhdvlct_batch* b, int i) {
     // untuned default: when the batch has too few column tiles to fill the
     // GPU (a few large blocks, e.g. one serving request), cut the columns
     // into z-chunks so that a stage has about two waves of tiles
-    static int nsm = 0;
-    if (nsm == 0) {
-      int dev = 0;
+    // SM count of the current device (thread-safe one-time initialisation)
+    static const int nsm = [] {
+      int dev = 0, n = 0;
       cudaGetDevice(&dev);
-      if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-          nsm <= 0)
-        nsm = 1;
-    }
+      if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          n <= 0)
+        n = 1;
+      return n;
+    }();
     const int target = 4 * nsm;
     for (int s = 0; s < 2; s++) {
       long columns = 0;
