@@ -58,7 +58,7 @@ def _args():
     ap.add_argument("--cpu-sample-blocks", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mode", default="main",
-                    choices=["main", "amr", "serve", "precision", "fc"],
+                    choices=["main", "amr", "serve", "precision", "fc", "smr"],
                     help="main: the contract line; amr / serve / precision: the "
                          "mixed-size block set, the serving stream, the FP32-vs-FP64 "
                          "study (one JSON line each)")
@@ -300,7 +300,7 @@ def view_pointers(v):
             "bfieldi_z": v.bfieldi[2]}
 
 
-def make_batch_general(meth, blocks, dims, widths, dtype, nbr):
+def make_batch_general(meth, blocks, dims, widths, dtype, nbr, ghost=GHOST):
     """Batch of arbitrary blocks: dims/widths per block, nbr the 27-neighbour
     table (nblocks x 27); blocks' host arrays are copied into the pool."""
     import numpy as np
@@ -310,7 +310,7 @@ def make_batch_general(meth, blocks, dims, widths, dtype, nbr):
     ws = (ctypes.c_double * (3 * n_blk))(*[float(x) for w in widths for x in w])
     h = ctypes.c_void_p()
     L = capi.lib()
-    capi.check(L.mhdvlct_batch_create(meth.handle, cd, ws, n_blk, GHOST, dtype,
+    capi.check(L.mhdvlct_batch_create(meth.handle, cd, ws, n_blk, ghost, dtype,
                                       ctypes.byref(h)), meth.handle, "batch_create")
     nbr = np.ascontiguousarray(nbr, dtype=np.int32)
     capi.check(L.mhdvlct_batch_set_neighbors(
@@ -464,6 +464,170 @@ def run_amr(a):
             "kernels_ms_per_step": dict(zip(("timestep", "refresh", "stage1_half_dt",
                                              "stage2_full_dt", "cycle"), list(prof))),
             "gpu_launches": 6 * a.steps, "clocks": clk,
+            "finite": all(np.isfinite(list(diag)))}
+
+
+SMR_GHOST = 4  # the reference's SMR decks (input/FluxCorrect/inclined_contact.incl)
+
+
+def smr_state(mesh, i, n, g, domain=1.0):
+    """Inclined density contact moving along (1,1,1) on leaf i (hydro): the
+    shape of the reference's hd_entropy inclined-wave SMR deck at a large
+    amplitude; ghosts left NaN for the first refresh to fill."""
+    import numpy as np
+    lvl, _ = mesh.leaves[i]
+    root_n = mesh.root[0] * n
+    h = domain / root_n / 2 ** lvl
+    fine = domain / root_n / 2 ** mesh.max_level
+    o = [x * fine for x in mesh.origin(i, (n, n, n))]
+    ax = [o[a] + (np.arange(n + 2 * g) - g + 0.5) * h for a in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    rho = 1.0 + 0.5 * np.sin(2 * np.pi * (x + y + z) / domain)
+    v = 0.5
+    p = 0.6
+    st = {"density": rho, "velocity_x": np.full_like(rho, v),
+          "velocity_y": np.full_like(rho, v), "velocity_z": np.full_like(rho, v),
+          "pressure": np.full_like(rho, p),
+          "total_energy": p / (2.0 / 3.0) / rho + 1.5 * v * v}
+    act = tuple(slice(g, g + n) for _ in range(3))
+    for k in st:
+        a = np.full_like(st[k], np.nan)
+        a[act] = st[k][act]
+        st[k] = a
+    return st, (h, h, h)
+
+
+def _smr_cpu(n=32, cycles=1):
+    """CPU oracle on a two-level sample: a 2^3 root grid of n^3 blocks with
+    one root block refined (15 leaves), refresh + dt + step per cycle, one
+    core.  Returns zone-updates/s."""
+    import numpy as np
+    from oracle import oracle as O
+    from mhdvlct import capi, mesh as M
+    mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
+    g = SMR_GHOST
+    prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=COURANT)
+    obs, slots = [], []
+    for i in range(len(mesh.leaves)):
+        st, w = smr_state(mesh, i, n, g)
+        ob = O.Block(n, g, w, mhd=False)
+        for k, v in st.items():
+            ob.f[{"density": "rho", "velocity_x": "vx", "velocity_y": "vy",
+                  "velocity_z": "vz", "total_energy": "etot",
+                  "pressure": "pressure"}[k]][...] = v
+        obs.append(ob)
+        slots.append({0: ob.f["rho"], 1: ob.f["vx"], 2: ob.f["vy"], 3: ob.f["vz"],
+                      4: ob.f["etot"], 9: ob.f["pressure"]})
+    faces = mesh.face_ints()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+    t0 = time.perf_counter()
+    for _ in range(cycles):
+        dt = min(O.timestep(prm, ob) for ob in obs)
+        O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+        for ob in obs:
+            O.step(prm, ob, dt)
+    el = time.perf_counter() - t0
+    return len(obs) * n ** 3 * cycles / el, len(obs)
+
+
+def run_smr(a, root=8, n=32):
+    """Static mesh refinement, two levels: a periodic root grid of root^3
+    blocks of n^3 whose central half along every axis is refined once, hydro
+    HLLC + PLM in FP32 with ghost depth 4 (the reference's SMR decks), one
+    global dt per cycle; the cycle (dt, mesh refresh with restriction and
+    prolongation, two stages) replayed as one CUDA graph."""
+    import numpy as np
+    import torch
+    from mhdvlct import block as B, capi, mesh as M
+    L = capi.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    lo, hi = root // 4, root - root // 4
+    mesh = M.Mesh((root,) * 3, refine=lambda lvl, c: all(lo <= x < hi for x in c))
+    g = SMR_GHOST
+    nleaf = len(mesh.leaves)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=COURANT)
+    dims = [(n, n, n)] * nleaf
+    widths = [(1.0 / (root * n) / 2 ** lvl,) * 3 for lvl, _ in mesh.leaves]
+    cd = (ctypes.c_int * (3 * nleaf))(*[n] * (3 * nleaf))
+    ws = (ctypes.c_double * (3 * nleaf))(*[x for w in widths for x in w])
+    h = ctypes.c_void_p()
+    capi.check(L.mhdvlct_batch_create(meth.handle, cd, ws, nleaf, g, capi.MHD_DTYPE_F32,
+                                      ctypes.byref(h)), meth.handle, "batch_create")
+    rt = _cudart()
+    for i in range(nleaf):
+        st, _ = smr_state(mesh, i, n, g)
+        v = capi.MhdBlockView()
+        capi.check(L.mhdvlct_batch_block_view(h, i, ctypes.byref(v)))
+        for k, p in view_pointers(v).items():
+            if p and k in st:
+                arr = np.ascontiguousarray(st[k], dtype=np.float32)
+                assert rt.cudaMemcpy(p, arr.ctypes.data, arr.nbytes, 1) == 0
+        if v.pressure:
+            arr = np.ascontiguousarray(st["pressure"], dtype=np.float32)
+            assert rt.cudaMemcpy(v.pressure, arr.ctypes.data, arr.nbytes, 1) == 0
+    farr, nf = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    capi.check(L.mhdvlct_batch_set_refresh_faces(h, farr, nf, cons), meth.handle, "faces")
+    capi.check(L.mhdvlct_batch_refresh(h, sp), meth.handle, "first refresh")
+    zones = nleaf * n ** 3
+    capi.check(L.mhdvlct_batch_run(h, a.warmup, 0, None, sp), meth.handle, "warmup")
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    capi.check(L.mhdvlct_batch_run(h, a.steps, 0, None, sp), meth.handle, "run")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = (ctypes.c_float * 5)()
+    capi.check(L.mhdvlct_batch_profile(h, a.steps, 0, prof, sp), meth.handle, "profile")
+    diag = (ctypes.c_double * 8)()
+    capi.check(L.mhdvlct_batch_diagnostics(h, diag, sp), meth.handle, "diag")
+    L.mhdvlct_batch_destroy(h)
+    # compulsory bytes of the refresh: every region's receiver cells written
+    # and sender cells read once, over the refreshed fields (rho, v, etot, p)
+    fields = 6
+    i3 = lambda t: (ctypes.c_int * 3)(*t)  # noqa: E731
+    out4 = [(ctypes.c_int * 3)() for _ in range(4)]
+    moved = 0
+    counts = {-1: 0, 0: 0, 1: 0}
+    for s_, r_, t, f, k in mesh.faces():
+        counts[t] += 1
+        if L.mhdvlct_refresh_face_box(i3((n,) * 3), i3((g,) * 3), i3((0, 0, 0)), t, i3(f),
+                                      i3(k), *out4) == 1:
+            moved += (int(np.prod(list(out4[1]))) + int(np.prod(list(out4[3]))))
+    rbytes = moved * fields * 4
+    r_ms = float(prof[1])
+    hbm, hbm_kind = _peaks()
+    cpu = None
+    if not a.no_cpu:
+        v_cpu, nb_cpu = _smr_cpu()
+        cpu = {"value": v_cpu, "unit": "zone-updates/s", "cores": 1, "kind": "port",
+               "sample": f"{nb_cpu} leaves of 32^3 (2^3 root grid, one root block "
+                         "refined), FP64 oracle, refresh + dt + step, 1 cycle"}
+    return {"mode": "smr", "metric": "zone-updates/s (static mesh refinement, 2 levels)",
+            "value": zones * a.steps / (ms / 1e3), "unit": "zone-updates/s",
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
+            "dtype": "f32", "data": "synthetic (inclined density contact)",
+            "config": {"workload": f"{nleaf} leaves of {n}^3 (+{g} ghosts): {root}^3 root "
+                                   f"grid, central {hi - lo}^3 refined once; HLLC+PLM "
+                                   "hydro, global dt",
+                       "zones_per_step": zones,
+                       "faces": {"same": counts[0], "to_finer": counts[1],
+                                 "to_coarser": counts[-1]}},
+            "kernels_ms_per_step": dict(zip(("timestep", "refresh", "stage1_half_dt",
+                                             "stage2_full_dt", "cycle"), list(prof))),
+            "refresh": {"algorithmic_bytes": rbytes,
+                        "achieved_gbs": rbytes / (r_ms * 1e-3) / 1e9 if r_ms > 0 else None,
+                        "peak_gbs": hbm, "peak_kind": hbm_kind,
+                        "frac": (rbytes / (r_ms * 1e-3) / 1e9 / hbm) if r_ms > 0 else None},
+            "cpu_baseline": cpu, "gpu_launches": 5 * a.steps, "clocks": clk,
             "finite": all(np.isfinite(list(diag)))}
 
 
@@ -655,6 +819,8 @@ def main():
                 out = {"mode": "serve", **run_serve(nreq=a.serve_requests)}
             elif a.mode == "fc":
                 out = run_fc(a)
+            elif a.mode == "smr":
+                out = run_smr(a)
             else:
                 out = run_precision(a, cycles=a.precision_cycles, N=a.precision_n)
             print(json.dumps(out), flush=True)

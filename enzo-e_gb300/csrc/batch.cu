@@ -71,6 +71,12 @@ struct mhdvlct_batch {
   int tile_tx[2] = {0, 0}, tile_ty[2] = {0, 0};
   int* d_queue = nullptr;     // 2 counters
   int* d_nbr = nullptr;
+  // mesh refresh from a face list (replaces the 27-neighbour same-level
+  // refresh when set): pointer tables of both face-buffer parities, the
+  // regions and their CTA chunks
+  char* d_rf = nullptr;
+  size_t rf_ptr[2] = {0, 0}, rf_items = 0, rf_chunks = 0;
+  int rf_nchunks = -1;  // -1: no face list
   double* d_dt = nullptr;     // per block
   double* d_dtmin = nullptr;
   double* d_time = nullptr;
@@ -294,6 +300,10 @@ cudaError_t launch_timestep_b(mhdvlct_batch* b, int global_min, cudaStream_t st)
 
 template <class R>
 cudaError_t launch_refresh_b(mhdvlct_batch* b, cudaStream_t st) {
+  if (b->rf_nchunks >= 0)
+    return launch_refresh_faces(b->dtype, b->d_rf + b->rf_items, b->d_rf + b->rf_chunks,
+                                b->rf_nchunks, (void* const*)(b->d_rf + b->rf_ptr[b->parity]),
+                                st);
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
@@ -430,6 +440,7 @@ extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
   for (int s = 0; s < 2; s++) cudaFree(b->d_tiles[s]);
   cudaFree(b->d_queue);
   cudaFree(b->d_nbr);
+  if (b->d_rf) cudaFree(b->d_rf);
   cudaFree(b->d_dt);
   cudaFree(b->d_dtmin);
   cudaFree(b->d_time);
@@ -440,8 +451,56 @@ extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
   return MHD_OK;
 }
 
+namespace {
+void fill_view(const mhdvlct_batch* b, int i, int parity, MhdBlockView* v);
+}
+
 extern "C" int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* v) {
   if (!b || !v || i < 0 || i >= b->nblocks) return MHD_ERR_INVALID;
+  fill_view(b, i, b->parity, v);
+  return MHD_OK;
+}
+
+extern "C" int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefreshFace* faces,
+                                               int nfaces, unsigned conservative) {
+  if (!b || nfaces < 0 || (nfaces > 0 && !faces)) return MHD_ERR_INVALID;
+  drop_graphs(b);
+  if (b->d_rf) cudaFree(b->d_rf);
+  b->d_rf = nullptr;
+  b->rf_nchunks = -1;
+  if (nfaces == 0) return MHD_OK;  // back to the 27-neighbour refresh
+  std::vector<MhdBlockView> views(b->nblocks);
+  RefreshPlan plan[2];
+  for (int p = 0; p < 2; p++) {
+    for (int i = 0; i < b->nblocks; i++) fill_view(b, i, p, &views[i]);
+    const int rc = plan_refresh(b->h, views.data(), b->nblocks, faces, nfaces, conservative,
+                                plan[p]);
+    if (rc != MHD_OK) return bfail(b, rc, b->h->err);
+  }
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t bp = plan[0].ptrs.size() * sizeof(void*);
+  b->rf_ptr[0] = 0;
+  b->rf_ptr[1] = up(bp);
+  b->rf_items = b->rf_ptr[1] + up(bp);
+  b->rf_chunks = b->rf_items + up(plan[0].items.size());
+  const size_t total = b->rf_chunks + plan[0].chunks.size() + 1;
+  std::vector<char> host(total, 0);
+  memcpy(host.data() + b->rf_ptr[0], plan[0].ptrs.data(), bp);
+  memcpy(host.data() + b->rf_ptr[1], plan[1].ptrs.data(), bp);
+  memcpy(host.data() + b->rf_items, plan[0].items.data(), plan[0].items.size());
+  memcpy(host.data() + b->rf_chunks, plan[0].chunks.data(), plan[0].chunks.size());
+  if (cudaMalloc((void**)&b->d_rf, total) != cudaSuccess) {
+    b->d_rf = nullptr;
+    return bfail(b, MHD_ERR_NOMEM, "refresh tables");
+  }
+  cudaError_t e = cudaMemcpy(b->d_rf, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  b->rf_nchunks = plan[0].nchunks;
+  return MHD_OK;
+}
+
+namespace {
+void fill_view(const mhdvlct_batch* b, int i, int parity, MhdBlockView* v) {
   std::memset(v, 0, sizeof(*v));
   const auto& O = b->off[i];
   const size_t esz = b->dtype == MHD_DTYPE_F64 ? 8 : 4;
@@ -461,11 +520,11 @@ extern "C" int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* v
   v->internal_energy = p(O.ext[F_EINT]);
   for (int d = 0; d < 3; d++) {
     v->bfield[d] = p(O.ext[F_BX + d]);
-    v->bfieldi[d] = p(b->parity == 0 ? O.fa[d] : O.fb[d]);
+    v->bfieldi[d] = p(parity == 0 ? O.fa[d] : O.fb[d]);
   }
   v->pressure = p(O.pres);
-  return MHD_OK;
 }
+}  // namespace
 
 extern "C" int mhdvlct_batch_set_neighbors(mhdvlct_batch* b, const int* nbr) {
   if (!b || !nbr) return MHD_ERR_INVALID;

@@ -346,6 +346,8 @@ extern "C" int mhdvlct_create(const MhdVlctParams* p, mhdvlct_handle** out) {
 extern "C" int mhdvlct_destroy(mhdvlct_handle* h) {
   if (!h) return MHD_ERR_INVALID;
   if (h->scratch) cudaFree(h->scratch);
+  if (h->rf_dev) cudaFree(h->rf_dev);
+  if (h->rf_done) cudaEventDestroy(h->rf_done);
   delete h;
   return MHD_OK;
 }
@@ -695,6 +697,31 @@ extern "C" int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, d
   cudaStream_t st = (cudaStream_t)stream;
   return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, fc, st)
                                    : block_step_t<float>(h, b, dt, fc, st);
+}
+
+extern "C" int mhdvlct_block_bfield_from_potential(mhdvlct_handle* h, const MhdBlockView* b,
+                                                   const double* ax, const double* ay,
+                                                   const double* az, void* stream) {
+  if (!h) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  if (!h->mhd) return fail(h, MHD_ERR_INVALID, "the block has no magnetic field");
+  if (!ax || !ay || !az) return fail(h, MHD_ERR_INVALID, "missing vector potential");
+  const int g = b->ghost[0];
+  const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (b->dtype == MHD_DTYPE_F64)
+    e = launch_bfield_from_potential<double>(
+        m[0], m[1], m[2], ax, ay, az, b->cell_width[0], b->cell_width[1], b->cell_width[2],
+        (double*)b->bfieldi[0], (double*)b->bfieldi[1], (double*)b->bfieldi[2],
+        (double*)b->bfield[0], (double*)b->bfield[1], (double*)b->bfield[2], st);
+  else
+    e = launch_bfield_from_potential<float>(
+        m[0], m[1], m[2], ax, ay, az, b->cell_width[0], b->cell_width[1], b->cell_width[2],
+        (float*)b->bfieldi[0], (float*)b->bfieldi[1], (float*)b->bfieldi[2],
+        (float*)b->bfield[0], (float*)b->bfield[1], (float*)b->bfield[2], st);
+  return e == cudaSuccess ? MHD_OK : cuda_fail(h, e, "bfield from potential");
 }
 
 extern "C" int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,

@@ -26,6 +26,11 @@ struct mhdvlct_handle {
   size_t scratch_bytes = 0;
   int tile = 0;                // tile extent used by the plain path
   int zchunk = 0;              // z-chunk length used by the plain path
+  // mesh-refresh tables (pointer table, regions, chunks), reused across calls
+  void* rf_dev = nullptr;
+  size_t rf_bytes = 0;
+  cudaEvent_t rf_done = nullptr;  // recorded after the last refresh launch
+  std::vector<char> rf_host;
 };
 
 namespace mhdint {
@@ -56,5 +61,21 @@ vlct::FieldSet<R> fieldset_of(const MhdBlockView* b);
 
 // Default tile extent for a precision (fits the shared-memory budget).
 int default_tile(int dtype, int solver, int recon, int de);
+
+// Mesh ghost refresh (refresh.cu): a validated plan of refresh faces over a
+// set of block views -- the per-block field pointer table and the device
+// records of the regions and their CTA chunks.
+struct RefreshPlan {
+  std::vector<void*> ptrs;  // MHD_NFIELD_SLOTS pointers per block
+  std::vector<char> items;  // region records
+  std::vector<char> chunks; // CTA chunk records
+  int nchunks = 0;
+  int dtype = MHD_DTYPE_F64;
+};
+int plan_refresh(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
+                 const MhdRefreshFace* faces, int nfaces, unsigned conservative,
+                 RefreshPlan& plan);
+cudaError_t launch_refresh_faces(int dtype, const void* d_items, const void* d_chunks,
+                                 int nchunks, void* const* d_ptrs, cudaStream_t st);
 
 }  // namespace mhdint

@@ -355,6 +355,67 @@ refresh_fast_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restric
   }
 }
 
+// Face-centred B from an edge-centred vector potential and the centred B
+// (EnzoInitialBCenter::initialize_bfield_interface / bfieldi_helper_,
+// src/Enzo/initial/EnzoInitialBCenter.cpp:41-127, then
+// initialize_bfield_center, :27-38): in double, cast to the block's type,
+//   Bx(k, j, i-1/2) = (Az(k, j+1/2) - Az(k, j-1/2)) / dy - (Ay(k+1/2, j) - Ay(k-1/2, j)) / dz
+// and the cyclic permutations.  A_x has extents (m0, m1+1, m2+1) along
+// (x, y, z), A_y (m0+1, m1, m2+1), A_z (m0+1, m1+1, m2), x fastest.
+template <class R>
+__global__ void bfield_from_potential_kernel(int m0, int m1, int m2, const double* ax,
+                                             const double* ay, const double* az, double dx,
+                                             double dy, double dz, R* bfx, R* bfy, R* bfz) {
+  const size_t fx = (size_t)(m0 + 1) * m1 * m2, fy = (size_t)m0 * (m1 + 1) * m2,
+               fz = (size_t)m0 * m1 * (m2 + 1);
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < fx + fy + fz;
+       q += (size_t)gridDim.x * blockDim.x) {
+    if (q < fx) {  // bfieldi_x (m2, m1, m0+1): Aj = Ay, Ak = Az, dj = dy, dk = dz
+      const size_t r = q;
+      const int i = (int)(r % (m0 + 1)), j = (int)((r / (m0 + 1)) % m1),
+                k = (int)(r / ((size_t)(m0 + 1) * m1));
+      const double akr = az[((size_t)k * (m1 + 1) + (j + 1)) * (m0 + 1) + i];
+      const double akl = az[((size_t)k * (m1 + 1) + j) * (m0 + 1) + i];
+      const double ajr = ay[((size_t)(k + 1) * m1 + j) * (m0 + 1) + i];
+      const double ajl = ay[((size_t)k * m1 + j) * (m0 + 1) + i];
+      bfx[r] = (R)(((akr - akl) / dy - (ajr - ajl) / dz));
+    } else if (q < fx + fy) {  // bfieldi_y (m2, m1+1, m0): Aj = Az, Ak = Ax, dj = dz, dk = dx
+      const size_t r = q - fx;
+      const int i = (int)(r % m0), j = (int)((r / m0) % (m1 + 1)),
+                k = (int)(r / ((size_t)m0 * (m1 + 1)));
+      const double akr = ax[((size_t)(k + 1) * (m1 + 1) + j) * m0 + i];
+      const double akl = ax[((size_t)k * (m1 + 1) + j) * m0 + i];
+      const double ajr = az[((size_t)k * (m1 + 1) + j) * (m0 + 1) + (i + 1)];
+      const double ajl = az[((size_t)k * (m1 + 1) + j) * (m0 + 1) + i];
+      bfy[r] = (R)(((akr - akl) / dz - (ajr - ajl) / dx));
+    } else {  // bfieldi_z (m2+1, m1, m0): Aj = Ax, Ak = Ay, dj = dx, dk = dy
+      const size_t r = q - fx - fy;
+      const int i = (int)(r % m0), j = (int)((r / m0) % m1), k = (int)(r / ((size_t)m0 * m1));
+      const double akr = ay[((size_t)k * m1 + j) * (m0 + 1) + (i + 1)];
+      const double akl = ay[((size_t)k * m1 + j) * (m0 + 1) + i];
+      const double ajr = ax[((size_t)k * (m1 + 1) + (j + 1)) * m0 + i];
+      const double ajl = ax[((size_t)k * (m1 + 1) + j) * m0 + i];
+      bfz[r] = (R)(((akr - akl) / dx - (ajr - ajl) / dy));
+    }
+  }
+}
+
+// compute_center_bfield over the whole block (EnzoBfieldMethodCT.cpp:702-728)
+template <class R>
+__global__ void center_bfield_kernel(int m0, int m1, int m2, const R* bfx, const R* bfy,
+                                     const R* bfz, R* bx, R* by, R* bz) {
+  const size_t M = (size_t)m0 * m1 * m2;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < M;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % m0), j = (int)((c / m0) % m1), k = (int)(c / ((size_t)m0 * m1));
+    const size_t ix = ((size_t)k * m1 + j) * (m0 + 1) + i;
+    const size_t iy = ((size_t)k * (m1 + 1) + j) * m0 + i;
+    bx[c] = R(0.5) * (bfx[ix] + bfx[ix + 1]);
+    by[c] = R(0.5) * (bfy[iy] + bfy[iy + m0]);
+    bz[c] = R(0.5) * (bfz[c] + bfz[c + (size_t)m0 * m1]);
+  }
+}
+
 // Copy the face-B box updated by the final stage (faces k in [lo, hi_d) along
 // d, transverse [lo, hi)) from the stage's face buffer into the caller's field.
 template <class R>

@@ -157,4 +157,17 @@ cudaError_t launch_diag<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, int nb, int g, 
   return cudaGetLastError();
 }
 
+template <>
+cudaError_t launch_bfield_from_potential<VLCT_REAL>(
+    int m0, int m1, int m2, const double* ax, const double* ay, const double* az,
+    double dx, double dy, double dz, VLCT_REAL* bfx, VLCT_REAL* bfy, VLCT_REAL* bfz,
+    VLCT_REAL* bx, VLCT_REAL* by, VLCT_REAL* bz, cudaStream_t st) {
+  bfield_from_potential_kernel<VLCT_REAL><<<1024, 256, 0, st>>>(m0, m1, m2, ax, ay, az, dx, dy,
+                                                               dz, bfx, bfy, bfz);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  center_bfield_kernel<VLCT_REAL><<<1024, 256, 0, st>>>(m0, m1, m2, bfx, bfy, bfz, bx, by, bz);
+  return cudaGetLastError();
+}
+
 }  // namespace vlct

@@ -51,6 +51,13 @@ cudaError_t launch_diag(const AuxBlock<R>* d_blocks, int nblocks, int g, int cpb
                         bool mhd, bool de, double* partial, double* out,
                         cudaStream_t st);
 
+// face B from an edge vector potential (double), then the centred B
+template <class R>
+cudaError_t launch_bfield_from_potential(int m0, int m1, int m2, const double* ax,
+                                         const double* ay, const double* az, double dx,
+                                         double dy, double dz, R* bfx, R* bfy, R* bfz,
+                                         R* bx, R* by, R* bz, cudaStream_t st);
+
 cudaError_t launch_set_scalar(double* p, double v, cudaStream_t st);
 
 }  // namespace vlct

@@ -224,6 +224,51 @@ class EnzoMethodMHDVlct:
         capi.check(rc, self.handle, "mhdvlct_block_timestep")
         return dt.value
 
+    def initialize_bfield_from_potential(self, block: Block, ax: torch.Tensor,
+                                         ay: torch.Tensor, az: torch.Tensor,
+                                         stream=None) -> None:
+        """Set the block's face and centred B from an edge-centred vector
+        potential (EnzoInitialBCenter::initialize_bfield_interface then
+        ::initialize_bfield_center, EnzoInitialBCenter.cpp:27-127).  ax, ay,
+        az are float64 device tensors of shapes (mz+1, my+1, mx),
+        (mz+1, my, mx+1) and (mz, my+1, mx+1)."""
+        mx, my, mz = (x + 2 * block.ghost for x in block.n)
+        for a, shp in ((ax, (mz + 1, my + 1, mx)), (ay, (mz + 1, my, mx + 1)),
+                       (az, (mz, my + 1, mx + 1))):
+            if (tuple(a.shape) != shp or a.dtype != torch.float64 or not a.is_cuda
+                    or not a.is_contiguous()):
+                raise ValueError(f"vector potential component must be a contiguous "
+                                 f"float64 device tensor of shape {shp}")
+        v = block.view()
+        rc = capi.lib().mhdvlct_block_bfield_from_potential(
+            self.handle, ctypes.byref(v), ax.data_ptr(), ay.data_ptr(), az.data_ptr(),
+            _stream_ptr(stream))
+        capi.check(rc, self.handle, "mhdvlct_block_bfield_from_potential")
+
+    def refresh_faces(self, blocks, faces, conservative=None, stream=None) -> None:
+        """Cello's ghost refresh over a mesh of blocks whose neighbours may be
+        one level coarser or finer (restrict / prolong, "linear"), all faces in
+        one launch.  `faces`: MhdRefreshFace records, as (array, count) from
+        mesh.Mesh.face_array() or a list of (sender, receiver, type, face,
+        child) tuples; `conservative`: field-slot mask of the density-weighted
+        fields (default: velocities and total energy)."""
+        if conservative is None:
+            conservative = capi.MHD_CONSERVATIVE_DEFAULT
+        if isinstance(faces, tuple) and len(faces) == 2 and not isinstance(faces[0], int):
+            arr, nf = faces
+        else:
+            nf = len(faces)
+            arr = (capi.MhdRefreshFace * max(1, nf))()
+            for i, (s, r, t, f, k) in enumerate(faces):
+                arr[i].sender, arr[i].receiver, arr[i].type = s, r, t
+                for a in range(3):
+                    arr[i].face[a], arr[i].child[a] = f[a], k[a]
+        views = (capi.MhdBlockView * len(blocks))(*[b.view() for b in blocks])
+        rc = capi.lib().mhdvlct_refresh_faces(self.handle, views, len(blocks), arr, nf,
+                                              ctypes.c_uint(conservative),
+                                              _stream_ptr(stream))
+        capi.check(rc, self.handle, "mhdvlct_refresh_faces")
+
     def fill_ghosts_periodic(self, block: Block, stream=None) -> None:
         v = block.view()
         rc = capi.lib().mhdvlct_fill_ghosts_periodic(self.handle, ctypes.byref(v),

@@ -29,10 +29,12 @@ EXPORTED = (
     "mhdvlct_destroy", "mhdvlct_last_error_string",
     "mhdvlct_courant", "mhdvlct_required_ghost_depth", "mhdvlct_block_step",
     "mhdvlct_block_step_noalloc", "mhdvlct_block_step_fc",
+    "mhdvlct_block_bfield_from_potential",
     "mhdvlct_block_timestep", "mhdvlct_fill_ghosts_periodic",
+    "mhdvlct_refresh_faces", "mhdvlct_refresh_face_box",
     "mhdvlct_batch_create", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
-    "mhdvlct_batch_refresh", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
+    "mhdvlct_batch_refresh", "mhdvlct_batch_set_refresh_faces", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
     "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_set_stage_tile",
     "mhdvlct_batch_autotune",
     "mhdvlct_batch_state_region", "mhdvlct_batch_profile",
@@ -63,6 +65,24 @@ class MhdFluxCorrection(ctypes.Structure):
 
 MHD_Q_DENSITY, MHD_Q_VELOCITY_X, MHD_Q_VELOCITY_Y, MHD_Q_VELOCITY_Z = 0, 1, 2, 3
 MHD_Q_TOTAL_ENERGY, MHD_Q_INTERNAL_ENERGY = 4, 5
+
+MHD_REFRESH_COARSE, MHD_REFRESH_SAME, MHD_REFRESH_FINE = -1, 0, 1
+# field slots of the mesh refresh (MHD_FIELD_* in the header)
+FIELD_SLOTS = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
+               "internal_energy", "bfield_x", "bfield_y", "bfield_z", "pressure",
+               "acceleration_x", "acceleration_y", "acceleration_z", "passive_0",
+               "passive_1", "passive_2", "passive_3", "bfieldi_x", "bfieldi_y",
+               "bfieldi_z")
+MHD_NFIELD_SLOTS = len(FIELD_SLOTS)
+MHD_CONSERVATIVE_DEFAULT = sum(1 << FIELD_SLOTS.index(k) for k in (
+    "velocity_x", "velocity_y", "velocity_z", "total_energy"))
+
+
+class MhdRefreshFace(ctypes.Structure):
+    """One (sender, receiver) pair of a mesh refresh, from the sender's side."""
+    _fields_ = [("sender", ctypes.c_int), ("receiver", ctypes.c_int),
+                ("type", ctypes.c_int), ("face", ctypes.c_int * 3),
+                ("child", ctypes.c_int * 3)]
 
 
 class MhdBlockView(ctypes.Structure):
@@ -121,13 +141,18 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_block_step.argtypes = [vp, P(MhdBlockView), dp, vp]
     L.mhdvlct_block_step_noalloc.argtypes = [vp, P(MhdBlockView), dp, vp]
     L.mhdvlct_block_step_fc.argtypes = [vp, P(MhdBlockView), dp, P(MhdFluxCorrection), vp]
+    L.mhdvlct_block_bfield_from_potential.argtypes = [vp, P(MhdBlockView), vp, vp, vp, vp]
     L.mhdvlct_block_timestep.argtypes = [vp, P(MhdBlockView), P(dp), vp]
     L.mhdvlct_fill_ghosts_periodic.argtypes = [vp, P(MhdBlockView), vp]
+    L.mhdvlct_refresh_faces.argtypes = [vp, P(MhdBlockView), ip, P(MhdRefreshFace), ip,
+                                        ctypes.c_uint, vp]
+    L.mhdvlct_refresh_face_box.argtypes = [P(ip)] * 3 + [ip] + [P(ip)] * 6
     L.mhdvlct_batch_create.argtypes = [vp, P(ip), P(dp), ip, ip, ip, P(vp)]
     L.mhdvlct_batch_destroy.argtypes = [vp]
     L.mhdvlct_batch_block_view.argtypes = [vp, ip, P(MhdBlockView)]
     L.mhdvlct_batch_set_neighbors.argtypes = [vp, P(ip)]
     L.mhdvlct_batch_refresh.argtypes = [vp, vp]
+    L.mhdvlct_batch_set_refresh_faces.argtypes = [vp, P(MhdRefreshFace), ip, ctypes.c_uint]
     L.mhdvlct_batch_step.argtypes = [vp, P(dp), vp]
     L.mhdvlct_batch_timestep.argtypes = [vp, P(dp), vp]
     L.mhdvlct_batch_run.argtypes = [vp, ip, ip, P(dp), vp]

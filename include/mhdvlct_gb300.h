@@ -172,11 +172,93 @@ int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
 int mhdvlct_block_step_noalloc(mhdvlct_handle* h, const MhdBlockView* b,
                                double dt, void* stream);
 
+/* Initial face-centred B as the curl of an edge-centred vector potential,
+ * then the centred B (EnzoInitialBCenter::initialize_bfield_interface and
+ * ::initialize_bfield_center, src/Enzo/initial/EnzoInitialBCenter.cpp:27-127):
+ * computed in double and cast to the block's type.  ax, ay, az are device
+ * arrays in double with extents (x, y, z) = (m0, m1+1, m2+1), (m0+1, m1,
+ * m2+1), (m0+1, m1+1, m2) for the ghosted extents m, x fastest. */
+int mhdvlct_block_bfield_from_potential(mhdvlct_handle* h, const MhdBlockView* b,
+                                        const double* ax, const double* ay,
+                                        const double* az, void* stream);
+
 /* Same-level periodic ghost refresh of a block onto itself (the effect of
  * Cello's refresh for a single periodic root block,
  * src/Cello/control_refresh.cpp:243-360). */
 int mhdvlct_fill_ghosts_periodic(mhdvlct_handle* h, const MhdBlockView* b,
                                  void* stream);
+
+/* ------------------------------------------------- mesh ghost refresh
+ * Cello's ghost refresh between the leaf blocks of a mesh whose neighbours
+ * may sit one level coarser or finer (Block::refresh_load_field_faces_ and
+ * refresh_load_field_face_, src/Cello/control_refresh.cpp:243-360; the
+ * per-face work of FieldFace::face_to_face, src/Cello/data_FieldFace.cpp:
+ * 440-566) with the "linear" operators: restriction (RestrictLinear,
+ * src/Cello/problem_RestrictLinear.cpp:53-196) into a coarser receiver and
+ * prolongation (ProlongLinear, src/Cello/problem_ProlongLinear.cpp:79-310)
+ * into a finer one.  One face is one (sender, receiver) pair as Cello's
+ * neighbour iterator yields it, described from the sender's side. */
+enum { MHD_REFRESH_COARSE = -1, MHD_REFRESH_SAME = 0, MHD_REFRESH_FINE = 1 };
+
+typedef struct MhdRefreshFace {
+  int sender;    /* index of the sending block in the blocks[] array        */
+  int receiver;  /* index of the receiving block                             */
+  int type;      /* the receiver's level relative to the sender's:
+                  * MHD_REFRESH_COARSE (restrict), _SAME (copy), _FINE
+                  * (prolong)                                                */
+  int face[3];   /* the sender's face toward the receiver, -1/0/+1 per axis  */
+  int child[3];  /* _COARSE: the sender's child index within its parent;
+                  * _FINE: the receiver's child index within its parent;
+                  * _SAME: ignored (0/1 per axis)                            */
+} MhdRefreshFace;
+
+/* Field slots, as used by the `conservative` mask below. */
+enum {
+  MHD_FIELD_DENSITY = 0,
+  MHD_FIELD_VELOCITY_X = 1, MHD_FIELD_VELOCITY_Y = 2, MHD_FIELD_VELOCITY_Z = 3,
+  MHD_FIELD_TOTAL_ENERGY = 4,
+  MHD_FIELD_INTERNAL_ENERGY = 5,
+  MHD_FIELD_BFIELD_X = 6, MHD_FIELD_BFIELD_Y = 7, MHD_FIELD_BFIELD_Z = 8,
+  MHD_FIELD_PRESSURE = 9,
+  MHD_FIELD_ACCELERATION_X = 10, MHD_FIELD_ACCELERATION_Y = 11,
+  MHD_FIELD_ACCELERATION_Z = 12,
+  MHD_FIELD_PASSIVE_0 = 13, /* .. MHD_FIELD_PASSIVE_0 + 3 */
+  MHD_FIELD_BFIELDI_X = 17, MHD_FIELD_BFIELDI_Y = 18, MHD_FIELD_BFIELDI_Z = 19,
+  MHD_NFIELD_SLOTS = 20
+};
+/* The "make_field_conservative" group of the reference's flux-correction
+ * decks (input/FluxCorrect/inclined_contact.incl): velocities and total
+ * energy are interpolated as density-weighted quantities across levels. */
+#define MHD_CONSERVATIVE_DEFAULT                                               \
+  ((1u << MHD_FIELD_VELOCITY_X) | (1u << MHD_FIELD_VELOCITY_Y) |               \
+   (1u << MHD_FIELD_VELOCITY_Z) | (1u << MHD_FIELD_TOTAL_ENERGY))
+
+/* Refresh the ghost zones named by `faces` in one launch.  Every block has the
+ * same active size, ghost depth and dtype (as in Cello); every field present
+ * (non-NULL) in the views is refreshed, density first.  Cell fields in the
+ * `conservative` mask (bit MHD_FIELD_*) are multiplied by the sender's
+ * density before a restriction or prolongation and divided by the receiver's
+ * refreshed density after it (FieldFace::mul_by_density_ / div_by_density_,
+ * data_FieldFace.cpp:863-980); the sender's own values are left untouched.
+ * Face-centred B is refreshed between same-level blocks only: the reference
+ * has no restriction or prolongation for it (its ProlongLinear rejects the
+ * face-centred extents).  Returns MHD_ERR_INVALID where the reference would
+ * assert: a prolongation whose fine extent is not twice the coarse one (odd
+ * ghost depth), mixed sizes, or an out-of-range index. */
+int mhdvlct_refresh_faces(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
+                          const MhdRefreshFace* faces, int nfaces,
+                          unsigned conservative, void* stream);
+
+/* The regions of one face (host only, no device work): the sender's cells
+ * read (send_start/send_size, array indices of the sender) and the
+ * receiver's ghost cells written (recv_start/recv_size), as Cello's Box
+ * computes them (src/Cello/mesh_Box.cpp:13-234) for a field of the given
+ * centering.  Returns 1 when the face has cells to refresh, 0 when not, and
+ * a negative value on a bad argument. */
+int mhdvlct_refresh_face_box(const int n[3], const int ghost[3], const int centering[3],
+                             int type, const int face[3], const int child[3],
+                             int send_start[3], int send_size[3], int recv_start[3],
+                             int recv_size[3]);
 
 /* ------------------------------------------------------------- batch
  * Many blocks of possibly different sizes advanced together: one fused,
@@ -199,6 +281,12 @@ int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* out);
 int mhdvlct_batch_set_neighbors(mhdvlct_batch* b, const int* nbr);
 /* Ghost refresh of every block from its neighbours. */
 int mhdvlct_batch_refresh(mhdvlct_batch* b, void* stream);
+/* Replace the batch's same-level refresh by the mesh refresh of `faces`
+ * (block indices of the batch; see mhdvlct_refresh_faces), planned once and
+ * replayed inside the cycle's CUDA graph.  nfaces = 0 restores the
+ * 27-neighbour refresh.  Every block must have the same extents. */
+int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefreshFace* faces,
+                                    int nfaces, unsigned conservative);
 /* One VL+CT step of every block; dt_per_block: host array of nblocks. */
 int mhdvlct_batch_step(mhdvlct_batch* b, const double* dt_per_block,
                        void* stream);

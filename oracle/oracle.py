@@ -49,12 +49,12 @@ class OracleBlock(ctypes.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle with the flags that keep the reference's FP order."""
-    src = os.path.join(HERE, "vlct_oracle.cpp")
-    if force or not os.path.exists(LIB_PATH) or (
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(src)):
+    srcs = [os.path.join(HERE, f) for f in ("vlct_oracle.cpp", "refresh_oracle.cpp")]
+    if force or not os.path.exists(LIB_PATH) or any(
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(s) for s in srcs):
         subprocess.check_call([
             "g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
-            "-fno-fast-math", "-o", LIB_PATH, src])
+            "-fno-fast-math", "-o", LIB_PATH] + srcs)
     return LIB_PATH
 
 
@@ -81,8 +81,28 @@ def ref_lib():
                                   ctypes.POINTER(_P), ctypes.c_int,
                                   ctypes.POINTER(ctypes.c_int)]
         L.ref_step_fc.restype = ctypes.c_int
+        L.ref_center_bfield.argtypes = [ctypes.c_int] * 3 + [_P] * 6
+        L.ref_center_bfield.restype = ctypes.c_int
         _ref = L
     return _ref
+
+
+REFRESH_REF_PATH = os.path.join(HERE, "_ref", "librefresh_ref.so")
+_refresh_ref = None
+
+
+def refresh_ref_lib():
+    """The reference's own Box / ProlongLinear / RestrictLinear built by
+    oracle/Makefile (only where the Enzo-E tree exists); None otherwise."""
+    global _refresh_ref
+    if _refresh_ref is None and os.path.exists(REFRESH_REF_PATH):
+        L = ctypes.CDLL(REFRESH_REF_PATH)
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.ref_refresh_box.argtypes = [ip] * 3 + [ctypes.c_int] + [ip] * 6
+        L.ref_refresh_faces.argtypes = [ctypes.c_int] * 2 + [ip] * 2 + [
+            ctypes.POINTER(ctypes.c_void_p), ip, ctypes.c_int, ctypes.c_uint]
+        _refresh_ref = L
+    return _refresh_ref
 
 
 def lib():
@@ -113,6 +133,10 @@ def lib():
                                              ctypes.POINTER(OracleBlock),
                                              ctypes.c_double, ctypes.c_int]
         L.oracle_evolve_periodic.restype = ctypes.c_int
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.oracle_refresh_box.argtypes = [ip] * 3 + [ctypes.c_int] + [ip] * 6
+        L.oracle_refresh_faces.argtypes = [ctypes.c_int] * 2 + [ip] * 2 + [
+            ctypes.POINTER(ctypes.c_void_p), ip, ctypes.c_int, ctypes.c_uint]
         _lib = L
     return _lib
 
@@ -294,3 +318,74 @@ def l1_error_norm(a: Block, b: Block, fields, gamma: float, res: int) -> float:
             x, y = a.f[k], b.f[k]
         errs.append(np.sum(np.abs(x[sl] - y[sl])) / float(res ** 3))
     return float(np.sqrt(np.sum(np.square(errs))))
+
+
+def bfield_from_potential(ax, ay, az, widths, dtype=np.float64):
+    """Face-centred and centred B of a ghosted block from an edge-centred
+    vector potential (float64 arrays in (z, y, x) order with the shapes
+    (mz+1, my+1, mx), (mz+1, my, mx+1), (mz, my+1, mx+1)).
+
+    Restates EnzoInitialBCenter::initialize_bfield_interface and
+    bfieldi_helper_ (src/Enzo/initial/EnzoInitialBCenter.cpp:41-127): each
+    face component is the curl difference evaluated in double, then cast to
+    the field type; the centred B is the mean of the two faces in the field
+    type (EnzoBfieldMethodCT::compute_center_bfield,
+    EnzoBfieldMethodCT.cpp:702-728)."""
+    dx, dy, dz = widths
+    mz, my, mx = az.shape[0], ay.shape[1], ax.shape[2]
+    # Bx(k, j, i-1/2) = (Az(k, j+1/2) - Az(k, j-1/2))/dy - (Ay(k+1/2, j) - Ay(k-1/2, j))/dz
+    bfx = ((az[:, 1:, :] - az[:, :-1, :]) / dy
+           - (ay[1:, :, :] - ay[:-1, :, :]) / dz).astype(dtype)
+    # By(k, j-1/2, i) = (Ax(k+1/2) - Ax(k-1/2))/dz - (Az(i+1/2) - Az(i-1/2))/dx
+    bfy = ((ax[1:, :, :] - ax[:-1, :, :]) / dz
+           - (az[:, :, 1:] - az[:, :, :-1]) / dx).astype(dtype)
+    # Bz(k-1/2, j, i) = (Ay(i+1/2) - Ay(i-1/2))/dx - (Ax(j+1/2) - Ax(j-1/2))/dy
+    bfz = ((ay[:, :, 1:] - ay[:, :, :-1]) / dx
+           - (ax[:, 1:, :] - ax[:, :-1, :]) / dy).astype(dtype)
+    assert bfx.shape == (mz, my, mx + 1) and bfy.shape == (mz, my + 1, mx)
+    assert bfz.shape == (mz + 1, my, mx)
+    half = dtype(0.5)
+    bx = half * (bfx[:, :, :-1] + bfx[:, :, 1:])
+    by = half * (bfy[:, :-1, :] + bfy[:, 1:, :])
+    bz = half * (bfz[:-1, :, :] + bfz[1:, :, :])
+    return (bfx, bfy, bfz), (bx, by, bz)
+
+
+# ----------------------------------------------------------- mesh refresh
+NFIELD_SLOTS = 20  # the C ABI's MHD_FIELD_* slot order
+
+
+def _i3(v):
+    return (ctypes.c_int * 3)(*[int(x) for x in v])
+
+
+def refresh_box(n, g, c, level, face, child, ref: bool = False):
+    """(send start, send size, receive start, receive size) of one face."""
+    L = refresh_ref_lib() if ref else lib()
+    out = [(ctypes.c_int * 3)() for _ in range(4)]
+    fn = L.ref_refresh_box if ref else L.oracle_refresh_box
+    rc = fn(_i3(n), _i3(g), _i3(c), int(level), _i3(face), _i3(child), *out)
+    if rc != 0:
+        raise RuntimeError("refresh_box failed")
+    return tuple(tuple(o) for o in out)
+
+
+def refresh_faces(blocks, n, g, faces, cons: int, ref: bool = False) -> None:
+    """Refresh in place.  blocks: list of dicts slot -> C-contiguous numpy
+    array (float64 or float32, all alike); faces: int array of 9 per face."""
+    dt = None
+    ptrs = (ctypes.c_void_p * (NFIELD_SLOTS * len(blocks)))()
+    for i, b in enumerate(blocks):
+        for s, a in b.items():
+            assert a.flags.c_contiguous
+            dt = a.dtype if dt is None else dt
+            assert a.dtype == dt
+            ptrs[NFIELD_SLOTS * i + s] = a.ctypes.data
+    faces = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 9)
+    L = refresh_ref_lib() if ref else lib()
+    fn = L.ref_refresh_faces if ref else L.oracle_refresh_faces
+    rc = fn(0 if dt == np.float64 else 1, len(blocks), _i3(n), _i3(g), ptrs,
+            faces.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(faces),
+            ctypes.c_uint(cons))
+    if rc != 0:
+        raise RuntimeError(f"refresh_faces failed: {rc}")

@@ -17,7 +17,6 @@ class er {
 };
 template <class T> inline void PUParray(er&, T*, int) {}
 }  // namespace PUP
-template <class T> inline void PUParray(PUP::er&, T*, int) {}
 class CkMigrateMessage;
 #define CkPrintf printf
 inline int CkMyPe() { return 0; }

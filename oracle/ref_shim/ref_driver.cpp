@@ -276,3 +276,24 @@ extern "C" double ref_timestep(const OracleParams* p, OracleBlock* b) {
     return -1.0;
   }
 }
+
+// Cell-centred B from face B over a whole block, through the reference's
+// EnzoBfieldMethodCT::compute_center_bfield (EnzoBfieldMethodCT.cpp:702-728)
+// with stale depth 0, as EnzoInitialBCenter::initialize_bfield_center does.
+extern "C" int ref_center_bfield(int mx, int my, int mz, double* bfx, double* bfy,
+                                 double* bfz, double* bx, double* by, double* bz) {
+  try {
+    double* bi[3] = {bfx, bfy, bfz};
+    double* bc[3] = {bx, by, bz};
+    for (int dim = 0; dim < 3; dim++) {
+      CelloView<enzo_float, 3> c(bc[dim], mz, my, mx);
+      CelloView<enzo_float, 3> f(bi[dim], mz + (dim == 2), my + (dim == 1), mx + (dim == 0));
+      CelloView<const enzo_float, 3> fc = f;
+      EnzoBfieldMethodCT::compute_center_bfield(dim, c, fc, 0);
+    }
+  } catch (const std::exception& e) {
+    fprintf(stderr, "ref_center_bfield: %s\n", e.what());
+    return 1;
+  }
+  return 0;
+}

@@ -34,3 +34,35 @@ def rel_l1(a, b):
     den = np.sum(np.abs(b))
     num = np.sum(np.abs(a - b))
     return 0.0 if den == 0 and num == 0 else num / max(den, 1e-300)
+
+
+# ------------------------------------------------------------ mesh refresh
+HYDRO_SLOTS = (0, 1, 2, 3, 4, 5, 9, 13)  # rho, v, etot, eint, pressure, passive_0
+MHD_SLOTS = HYDRO_SLOTS + (6, 7, 8, 17, 18, 19)
+
+
+def mesh_blocks(nblocks, n, g, slots, dtype, seed, rho_pow2=False):
+    """Per block a dict slot -> array in Cello's layout: random active cells
+    (density positive; a power of two when rho_pow2), NaN ghosts."""
+    rng = np.random.default_rng(seed)
+    m = [x + 2 * g for x in n]
+    out = []
+    for _ in range(nblocks):
+        b = {}
+        for s in slots:
+            shp = [m[2], m[1], m[0]]
+            if s >= 17:
+                shp[2 - (s - 17)] += 1
+            a = np.full(shp, np.nan, dtype=dtype)
+            # numpy axis k holds the spatial axis 2 - k; faces add one along theirs
+            act = tuple(slice(g, g + n[2 - k] + (1 if s >= 17 and 2 - k == s - 17 else 0))
+                        for k in range(3))
+            if s == 0:
+                v = (2.0 ** rng.integers(-3, 4, size=a[act].shape) if rho_pow2
+                     else 0.5 + rng.random(a[act].shape))
+            else:
+                v = rng.standard_normal(a[act].shape)
+            a[act] = v.astype(dtype)
+            b[s] = a
+        out.append(b)
+    return out

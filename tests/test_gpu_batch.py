@@ -23,12 +23,12 @@ KEYS = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
 
 
 class Batch:
-    def __init__(self, meth, dims, widths, dtype=capi.MHD_DTYPE_F64):
+    def __init__(self, meth, dims, widths, dtype=capi.MHD_DTYPE_F64, ghost=3):
         n = len(dims)
         d = (ctypes.c_int * (3 * n))(*[int(v) for t in dims for v in t])
         w = (ctypes.c_double * (3 * n))(*[float(v) for t in widths for v in t])
         h = ctypes.c_void_p()
-        rc = capi.lib().mhdvlct_batch_create(meth.handle, d, w, n, 3, dtype,
+        rc = capi.lib().mhdvlct_batch_create(meth.handle, d, w, n, ghost, dtype,
                                              ctypes.byref(h))
         capi.check(rc, meth.handle, "batch_create")
         self.h, self.meth, self.n = h, meth, n
