@@ -64,6 +64,8 @@ def _args():
                          "study (one JSON line each)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--smr-root", type=int, default=8,
+                    help="smr mode: root blocks per axis (the central half is refined)")
     ap.add_argument("--precision-n", type=int, default=512)
     ap.add_argument("--precision-cycles", type=int, default=50)
     ap.add_argument("--tile", type=str, default="",
@@ -820,7 +822,7 @@ def main():
             elif a.mode == "fc":
                 out = run_fc(a)
             elif a.mode == "smr":
-                out = run_smr(a)
+                out = run_smr(a, root=a.smr_root)
             else:
                 out = run_precision(a, cycles=a.precision_cycles, N=a.precision_n)
             print(json.dumps(out), flush=True)

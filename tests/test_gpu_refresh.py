@@ -205,4 +205,3 @@ def test_smr_batch_graph_bit_exact():
         got = bt.download(i)
         for k in ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy"):
             assert np.array_equal(got[k], ob.f[ic.ORACLE_NAME[k]], equal_nan=True), (i, k)
-    L.mhdvlct_batch_destroy(bt.h)
