@@ -175,8 +175,23 @@ template <class T>
 __global__ void __launch_bounds__(CHUNK)
     refresh_faces_kernel(const RefItem* __restrict__ items, const RefChunk* __restrict__ chunks,
                          void* const* __restrict__ ptrs) {
+  // the CTA's region record and both blocks' field pointers, staged once
+  __shared__ RefItem it;
+  __shared__ const T* src[NCELLSLOT];
+  __shared__ T* dst[NCELLSLOT];
   const RefChunk ck = chunks[blockIdx.x];
-  const RefItem& it = items[ck.item];
+  static_assert(sizeof(RefItem) % sizeof(int) == 0, "RefItem is copied as ints");
+  constexpr int NW = sizeof(RefItem) / sizeof(int);
+  if (threadIdx.x < NW)
+    ((int*)&it)[threadIdx.x] = ((const int*)(items + ck.item))[threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x < NCELLSLOT) {
+    const int j = threadIdx.x;
+    const bool in = j < it.nslot;
+    src[j] = in ? (const T*)ptrs[(size_t)NSLOT * it.sblk + it.slot0 + j] : nullptr;
+    dst[j] = in ? (T*)ptrs[(size_t)NSLOT * it.rblk + it.slot0 + j] : nullptr;
+  }
+  __syncthreads();
   const int q = ck.start + (int)threadIdx.x;
   if (q >= it.ncell) return;
   const int fx = q % it.nd[0];
@@ -185,68 +200,62 @@ __global__ void __launch_bounds__(CHUNK)
   const size_t rsy = (size_t)it.rm[0], rsz = (size_t)it.rm[0] * it.rm[1];
   const size_t ssy = (size_t)it.sm[0], ssz = (size_t)it.sm[0] * it.sm[1];
   const size_t ir = (size_t)(it.id[0] + fx) + rsy * (it.id[1] + fy) + rsz * (it.id[2] + fz);
-  void* const* sp = ptrs + (size_t)NSLOT * it.sblk;
-  void* const* rp = ptrs + (size_t)NSLOT * it.rblk;
-  const int s1 = it.slot0 + it.nslot;
+  // every value is loaded before anything is stored, so the loads of all
+  // fields are in flight together (the regions read and written never
+  // overlap)
+  T out[NCELLSLOT];
 
   if (it.type == 0) {
     const size_t is = (size_t)(it.is[0] + fx) + ssy * (it.is[1] + fy) + ssz * (it.is[2] + fz);
-    for (int s = it.slot0; s < s1; s++) {
-      const T* src = (const T*)sp[s];
-      if (src) ((T*)rp[s])[ir] = src[is];
-    }
-    return;
-  }
-  const T* rho_s = (const T*)sp[MHD_FIELD_DENSITY];
-  T rho_r = T(0);
-  if (it.type == -1) {
-    // the 2x2x2 fine cells under coarse cell (fx, fy, fz), in the reference's
-    // summation order: x, y, x+y, z, x+z, y+z, x+y+z
-    const size_t i0 =
-        (size_t)(it.is[0] + 2 * fx) + ssy * (it.is[1] + 2 * fy) + ssz * (it.is[2] + 2 * fz);
-    const size_t off[8] = {0, 1, ssy, 1 + ssy, ssz, 1 + ssz, ssy + ssz, 1 + ssy + ssz};
-    for (int s = it.slot0; s < s1; s++) {
-      const T* src = (const T*)sp[s];
-      if (!src) continue;
-      const bool cons = (it.cons >> s) & 1u;
-      T sum = T(0);
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        const T v = cons ? mul_rn(src[i0 + off[k]], rho_s[i0 + off[k]]) : src[i0 + off[k]];
-        sum = k == 0 ? v : add_rn(sum, v);
-      }
-      T out = mul_rn(T(0.125), sum);
-      if (s == MHD_FIELD_DENSITY) rho_r = out;
-      if (cons) out = div_rn(out, rho_r);
-      ((T*)rp[s])[ir] = out;
-    }
+    for (int j = 0; j < NCELLSLOT; j++)
+      if (src[j]) out[j] = src[j][is];
+#pragma unroll
+    for (int j = 0; j < NCELLSLOT; j++)
+      if (src[j]) dst[j][ir] = out[j];
     return;
   }
-  // prolongation
-  T wx[2], wy[2], wz[2];
-  const int icx = prolong_axis<T>(fx, it.nd[0], it.gc[0], wx[0], wx[1]);
-  const int icy = prolong_axis<T>(fy, it.nd[1], it.gc[1], wy[0], wy[1]);
-  const int icz = prolong_axis<T>(fz, it.nd[2], it.gc[2], wz[0], wz[1]);
-  const size_t i0 = (size_t)(it.is[0] + icx) + ssy * (it.is[1] + icy) + ssz * (it.is[2] + icz);
-  const size_t off[8] = {0, 1, ssy, 1 + ssy, ssz, 1 + ssz, ssy + ssz, 1 + ssy + ssz};
+  size_t i0;
   T w[8];
+  if (it.type == -1) {
+    // the 2x2x2 fine cells under coarse cell (fx, fy, fz)
+    i0 = (size_t)(it.is[0] + 2 * fx) + ssy * (it.is[1] + 2 * fy) + ssz * (it.is[2] + 2 * fz);
+  } else {
+    T wx[2], wy[2], wz[2];
+    const int icx = prolong_axis<T>(fx, it.nd[0], it.gc[0], wx[0], wx[1]);
+    const int icy = prolong_axis<T>(fy, it.nd[1], it.gc[1], wy[0], wy[1]);
+    const int icz = prolong_axis<T>(fz, it.nd[2], it.gc[2], wz[0], wz[1]);
+    i0 = (size_t)(it.is[0] + icx) + ssy * (it.is[1] + icy) + ssz * (it.is[2] + icz);
 #pragma unroll
-  for (int k = 0; k < 8; k++)
-    w[k] = mul_rn(mul_rn(wx[k & 1], wy[(k >> 1) & 1]), wz[(k >> 2) & 1]);
-  for (int s = it.slot0; s < s1; s++) {
-    const T* src = (const T*)sp[s];
-    if (!src) continue;
-    const bool cons = (it.cons >> s) & 1u;
+    for (int k = 0; k < 8; k++)
+      w[k] = mul_rn(mul_rn(wx[k & 1], wy[(k >> 1) & 1]), wz[(k >> 2) & 1]);
+  }
+  // the eight source cells in the reference's summation order: x, y, x+y,
+  // z, x+z, y+z, x+y+z
+  const size_t off[8] = {0, 1, ssy, 1 + ssy, ssz, 1 + ssz, ssy + ssz, 1 + ssy + ssz};
+  T rho8[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) rho8[k] = src[MHD_FIELD_DENSITY][i0 + off[k]];
+#pragma unroll
+  for (int j = 0; j < NCELLSLOT; j++) {
+    if (!src[j]) continue;
+    const bool cons = (it.cons >> j) & 1u;
     T sum = T(0);
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      const T v = cons ? mul_rn(src[i0 + off[k]], rho_s[i0 + off[k]]) : src[i0 + off[k]];
-      const T t = mul_rn(w[k], v);
+      const T raw = j == MHD_FIELD_DENSITY ? rho8[k] : src[j][i0 + off[k]];
+      const T v = cons ? mul_rn(raw, rho8[k]) : raw;
+      const T t = it.type == -1 ? v : mul_rn(w[k], v);
       sum = k == 0 ? t : add_rn(sum, t);
     }
-    if (s == MHD_FIELD_DENSITY) rho_r = sum;
-    if (cons) sum = div_rn(sum, rho_r);
-    ((T*)rp[s])[ir] = sum;
+    out[j] = it.type == -1 ? mul_rn(T(0.125), sum) : sum;
+  }
+  const T rho_r = out[MHD_FIELD_DENSITY];
+#pragma unroll
+  for (int j = 0; j < NCELLSLOT; j++) {
+    if (!src[j]) continue;
+    const bool cons = (it.cons >> j) & 1u;
+    dst[j][ir] = cons ? div_rn(out[j], rho_r) : out[j];
   }
 }
 
