@@ -205,3 +205,31 @@ def test_smr_batch_graph_bit_exact():
         got = bt.download(i)
         for k in ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy"):
             assert np.array_equal(got[k], ob.f[ic.ORACLE_NAME[k]], equal_nan=True), (i, k)
+
+
+def test_smr_batch_fp32_close_to_fp64_oracle():
+    # the benchmarked form: FP32 batch, mesh refresh inside the cycle graph,
+    # two cycles against the FP64 oracle (relative L1 over the active cells)
+    from test_gpu_batch import Batch
+    mesh, n, g, states, widths = _smr_case(False)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    prm = oracle_params("hllc", "plm", courant=0.4)
+    L = capi.lib()
+    bt = Batch(meth, [n] * len(states), widths, dtype=capi.MHD_DTYPE_F32, ghost=g)
+    for i, st in enumerate(states):
+        bt.upload(i, st)
+    farr, nf = mesh.face_array()
+    capi.check(L.mhdvlct_batch_set_refresh_faces(bt.h, farr, nf,
+                                                 capi.MHD_CONSERVATIVE_DEFAULT),
+               meth.handle, "faces")
+    capi.check(L.mhdvlct_batch_refresh(bt.h, None), meth.handle, "refresh")
+    capi.check(L.mhdvlct_batch_run(bt.h, 2, 0, None, None), meth.handle, "run")
+    oblocks = _oracle_smr(mesh, n, g, states, widths, False, prm, 2)
+    act = tuple(slice(g, g + k) for k in n[::-1])
+    for i, ob in enumerate(oblocks):
+        got = bt.download(i)
+        for k in ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy"):
+            want = ob.f[ic.ORACLE_NAME[k]][act]
+            err = np.abs(got[k][act].astype(np.float64) - want).sum() / np.abs(want).sum()
+            assert err <= 1e-5, (i, k, err)
