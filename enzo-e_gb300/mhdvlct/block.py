@@ -269,6 +269,30 @@ class EnzoMethodMHDVlct:
                                               _stream_ptr(stream))
         capi.check(rc, self.handle, "mhdvlct_refresh_faces")
 
+    def flux_correct(self, blocks, buffers, faces, conservative=None, stream=None) -> None:
+        """Cello's "flux_correct" Method over a mesh after a step that stored
+        the boundary fluxes: every coarse block's boundary cells next to finer
+        blocks are corrected by the difference between its own fluxes and its
+        finer neighbours' coarsened ones.  `buffers`: one FluxBuffers per
+        block (as compute_store_fluxes filled them); `faces`: the mesh's
+        refresh faces (mesh.Mesh.face_array() or a list of tuples)."""
+        if conservative is None:
+            conservative = capi.MHD_CONSERVATIVE_DEFAULT
+        if isinstance(faces, tuple) and len(faces) == 2 and not isinstance(faces[0], int):
+            arr, nf = faces
+        else:
+            nf = len(faces)
+            arr = (capi.MhdRefreshFace * max(1, nf))()
+            for i, (s_, r, t, f, k) in enumerate(faces):
+                arr[i].sender, arr[i].receiver, arr[i].type = s_, r, t
+                for a in range(3):
+                    arr[i].face[a], arr[i].child[a] = f[a], k[a]
+        views = (capi.MhdBlockView * len(blocks))(*[b.view() for b in blocks])
+        fcs = (capi.MhdFluxCorrection * len(blocks))(*[bf.fc for bf in buffers])
+        rc = capi.lib().mhdvlct_flux_correct(self.handle, views, len(blocks), fcs, arr, nf,
+                                             ctypes.c_uint(conservative), _stream_ptr(stream))
+        capi.check(rc, self.handle, "mhdvlct_flux_correct")
+
     def fill_ghosts_periodic(self, block: Block, stream=None) -> None:
         v = block.view()
         rc = capi.lib().mhdvlct_fill_ghosts_periodic(self.handle, ctypes.byref(v),

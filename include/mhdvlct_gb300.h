@@ -249,6 +249,27 @@ int mhdvlct_refresh_faces(mhdvlct_handle* h, const MhdBlockView* blocks, int nbl
                           const MhdRefreshFace* faces, int nfaces,
                           unsigned conservative, void* stream);
 
+/* Flux correction at coarse-fine faces: Cello's "flux_correct" Method, run
+ * after a step whose boundary fluxes were stored (mhdvlct_block_step_fc):
+ *   - each finer block's stored fluxes through its face toward a coarser
+ *     neighbour are coarsened onto that neighbour's face
+ *     (FaceFluxes::coarsen, src/Cello/data_FaceFluxes.cpp:128-252) and
+ *     summed (FluxData::sum_neighbor_fluxes, data_FluxData.hpp:132-145);
+ *   - the coarse block's boundary cells on such faces get
+ *     (2 face - 1) (own flux - neighbour flux) added, density first, the
+ *     `conservative` fields as density-weighted values divided by the
+ *     corrected density (MethodFluxCorrect::flux_correct_,
+ *     src/Cello/problem_MethodFluxCorrect.cpp:293-558).
+ * fluxes: one MhdFluxCorrection per block (host array of device pointers)
+ * holding the fluxes the step stored; every block stores the same
+ * quantities.  faces: the mesh's refresh faces (mhdvlct_refresh_faces); the
+ * axis faces of type MHD_REFRESH_COARSE are the ones used.  Cell fields
+ * updated: density, velocity_x/y/z (momentum fluxes), total_energy,
+ * internal_energy, as stored. */
+int mhdvlct_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
+                         const MhdFluxCorrection* fluxes, const MhdRefreshFace* faces,
+                         int nfaces, unsigned conservative, void* stream);
+
 /* The regions of one face (host only, no device work): the sender's cells
  * read (send_start/send_size, array indices of the sender) and the
  * receiver's ghost cells written (recv_start/recv_size), as Cello's Box

@@ -49,7 +49,8 @@ class OracleBlock(ctypes.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle with the flags that keep the reference's FP order."""
-    srcs = [os.path.join(HERE, f) for f in ("vlct_oracle.cpp", "refresh_oracle.cpp")]
+    srcs = [os.path.join(HERE, f) for f in ("vlct_oracle.cpp", "refresh_oracle.cpp",
+                                            "fluxcorrect_oracle.cpp")]
     if force or not os.path.exists(LIB_PATH) or any(
             os.path.getmtime(LIB_PATH) < os.path.getmtime(s) for s in srcs):
         subprocess.check_call([
@@ -101,6 +102,8 @@ def refresh_ref_lib():
         L.ref_refresh_box.argtypes = [ip] * 3 + [ctypes.c_int] + [ip] * 6
         L.ref_refresh_faces.argtypes = [ctypes.c_int] * 2 + [ip] * 2 + [
             ctypes.POINTER(ctypes.c_void_p), ip, ctypes.c_int, ctypes.c_uint]
+        L.ref_coarsen_fluxes.argtypes = [ip, ctypes.c_int, ctypes.c_int, ip,
+                                         ctypes.c_void_p, ctypes.c_void_p]
         _refresh_ref = L
     return _refresh_ref
 
@@ -137,6 +140,12 @@ def lib():
         L.oracle_refresh_box.argtypes = [ip] * 3 + [ctypes.c_int] + [ip] * 6
         L.oracle_refresh_faces.argtypes = [ctypes.c_int] * 2 + [ip] * 2 + [
             ctypes.POINTER(ctypes.c_void_p), ip, ctypes.c_int, ctypes.c_uint]
+        vpp = ctypes.POINTER(ctypes.c_void_p)
+        L.oracle_flux_correct.argtypes = [ctypes.c_int] * 2 + [ip] * 2 + [
+            vpp, vpp, ip, ctypes.c_int, ctypes.c_uint]
+        L.oracle_coarsen_fluxes.argtypes = [ctypes.c_int] * 3 + [
+            ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_coarsen_fluxes.restype = None
         _lib = L
     return _lib
 
@@ -389,3 +398,53 @@ def refresh_faces(blocks, n, g, faces, cons: int, ref: bool = False) -> None:
             ctypes.c_uint(cons))
     if rc != 0:
         raise RuntimeError(f"refresh_faces failed: {rc}")
+
+
+# -------------------------------------------------------- flux correction
+FC_FIELDS = ("rho", "vx", "vy", "vz", "etot", "eint")  # MHD_Q_* order
+
+
+def coarsen_fluxes(fine, ci, co, ref: bool = False, n=None, axis=0, face=0):
+    """FaceFluxes::coarsen of one fine face array (outer x inner, inner
+    fastest) for a child with transverse child index (ci, co).  The
+    reference's version (ref=True, FP64) needs the block extents n, the axis
+    and the face, and takes the child index per axis."""
+    fine = np.ascontiguousarray(fine)
+    out = np.zeros_like(fine)
+    if ref:
+        c3 = [0, 0, 0]
+        a_in = 1 if axis == 0 else 0
+        a_out = 1 if axis == 2 else 2
+        c3[a_in], c3[a_out] = ci, co
+        rc = refresh_ref_lib().ref_coarsen_fluxes(_i3(n), axis, face, _i3(c3),
+                                                  fine.ctypes.data, out.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("ref_coarsen_fluxes failed")
+        return out
+    no, ni = fine.shape
+    lib().oracle_coarsen_fluxes(0 if fine.dtype == np.float64 else 1, ni, no,
+                                fine.ctypes.data, ci, co, out.ctypes.data)
+    return out
+
+
+def flux_correct(blocks, fluxes, n, g, faces, cons: int) -> None:
+    """Correct in place.  blocks: list of dicts MHD_Q index -> array;
+    fluxes: list of dicts (axis, side, q) -> stored flux array (as step_fc
+    returns them); faces: int array of 9 per face."""
+    nb = len(blocks)
+    fp = (ctypes.c_void_p * (6 * nb))()
+    xp = (ctypes.c_void_p * (36 * nb))()
+    dt = None
+    for i, b in enumerate(blocks):
+        for q, a in b.items():
+            dt = a.dtype if dt is None else dt
+            fp[6 * i + q] = a.ctypes.data
+        for (ax, side, q), a in fluxes[i].items():
+            assert a.flags.c_contiguous and a.dtype == dt
+            xp[36 * i + (ax * 2 + side) * 6 + q] = a.ctypes.data
+    faces = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 9)
+    rc = lib().oracle_flux_correct(0 if dt == np.float64 else 1, nb, _i3(n), _i3(g), fp, xp,
+                                   faces.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                   len(faces), ctypes.c_uint(cons))
+    if rc != 0:
+        raise RuntimeError(f"flux_correct failed: {rc}")

@@ -49,6 +49,7 @@ class Block {
   virtual ~Block() {}
   bool is_leaf() const { return true; }
   double time() const { return 0.0; }
+  std::string name() const { return "block"; }
 };
 class FieldDescr {
  public:

@@ -10,7 +10,9 @@
  * Block::refresh_load_field_face_ (control_refresh.cpp:331-360: no ghost
  * flags, not accumulating).  Density weighting multiplies and divides the
  * sender's cells in place exactly as mul_by_density_ / div_by_density_ do
- * (data_FieldFace.cpp:863-980).  Built into oracle/_ref/ only where the
+ * (data_FieldFace.cpp:863-980).  It also exposes FaceFluxes::coarsen
+ * (data_FaceFluxes.cpp:128-252), the flux coarsening of the flux
+ * correction.  Built into oracle/_ref/ only where the
  * Enzo-E sources are present; never shipped or called by the product.
  */
 #include <cstdarg>
@@ -18,6 +20,7 @@
 
 #include "include_refresh/mesh.hpp"
 #include "include_refresh/problem.hpp"
+#include "include_refresh/data.hpp"
 
 void cello::message(FILE* fp, const char* type, const char* file, int line,
                     const char* function, const char* message, ...) {
@@ -153,4 +156,28 @@ extern "C" int ref_refresh_faces(int dtype, int nblocks, const int n[3], const i
     fprintf(stderr, "ref_refresh_faces: %s\n", e.what());
     return -1;
   }
+}
+
+// FaceFluxes::coarsen of one fine face array: a FaceFluxes on the given axis
+// face of a block of n cells, filled with `fine` (inner index fastest), then
+// coarsened for the child index c3; out receives the array after the call.
+extern "C" int ref_coarsen_fluxes(const int n[3], int axis, int face, const int c3[3],
+                                  const double* fine, double* out) {
+  try {
+    int f3[3] = {0, 0, 0};
+    f3[axis] = face == 0 ? -1 : 1;
+    Face fc(f3[0], f3[1], f3[2], axis, face);
+    FaceFluxes ff(fc, 0, n[0], n[1], n[2], 0, 0, 0);
+    ff.allocate_storage();
+    int mx, my, mz;
+    const int m = ff.get_size(&mx, &my, &mz);
+    double* a = ff.flux_array();
+    for (int i = 0; i < m; i++) a[i] = fine[i];
+    ff.coarsen(c3[0], c3[1], c3[2], 3);
+    for (int i = 0; i < m; i++) out[i] = a[i];
+  } catch (const std::exception& e) {
+    fprintf(stderr, "ref_coarsen_fluxes: %s\n", e.what());
+    return -1;
+  }
+  return 0;
 }

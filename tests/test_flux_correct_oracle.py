@@ -1,0 +1,103 @@
+"""Flux correction at coarse-fine faces on the CPU (Cello's "flux_correct"
+Method after a VL+CT step that stored its boundary fluxes):
+
+  - the oracle's coarsening of a finer block's face fluxes equals the
+    reference's own FaceFluxes::coarsen (src/Cello/data_FaceFluxes.cpp),
+    compiled here, bit for bit, for every axis, side and child quarter;
+  - a static-mesh-refinement run of the oracle (mesh refresh, step with
+    stored fluxes, flux correction; periodic, hydro) conserves mass,
+    momentum and total energy to round-off, as the reference's SMR VL
+    regression (FluxCorrect-SMR-VL, min_digits about 16 in FP64) expects,
+    and without the correction it does not.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from mhdvlct import capi, mesh as M
+
+N3 = (8, 6, 4)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("face", [0, 1])
+def test_coarsen_matches_reference(axis, face):
+    if O.refresh_ref_lib() is None:
+        pytest.skip("reference sources not built here")
+    a_in = 1 if axis == 0 else 0
+    a_out = 1 if axis == 2 else 2
+    ni, no = N3[a_in], N3[a_out]
+    rng = np.random.default_rng(7 * axis + face)
+    for ci, co in itertools.product((0, 1), repeat=2):
+        fine = rng.standard_normal((no, ni))
+        mine = O.coarsen_fluxes(fine, ci, co)
+        ref = O.coarsen_fluxes(fine, ci, co, ref=True, n=N3, axis=axis, face=face)
+        assert np.array_equal(mine, ref), (ci, co)
+        assert np.count_nonzero(mine) == (ni // 2) * (no // 2)
+
+
+def smr_blocks(n=8, g=4):
+    """A moving density contact on a 2x2x2 periodic root grid with one root
+    block refined: oracle blocks (hydro) and their cell volumes."""
+    mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
+    blocks, vols = [], []
+    for i, (lvl, _) in enumerate(mesh.leaves):
+        h = 1.0 / (2 * n) / 2 ** lvl
+        fine = 1.0 / (2 * n) / 2 ** mesh.max_level
+        o = [x * fine for x in mesh.origin(i, (n, n, n))]
+        ax = [o[a] + (np.arange(n + 2 * g) - g + 0.5) * h for a in range(3)]
+        z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+        b = O.Block(n, g, (h, h, h), mhd=False)
+        rho = 1.0 + 0.5 * np.sin(2 * np.pi * (x + 2 * y + 3 * z))
+        b.f["rho"][...] = rho
+        b.f["vx"][...] = 0.4
+        b.f["vy"][...] = -0.3
+        b.f["vz"][...] = 0.2
+        b.f["etot"][...] = 0.6 / (2.0 / 3.0) / rho + 0.5 * (0.16 + 0.09 + 0.04)
+        blocks.append(b)
+        vols.append(h ** 3)
+    return mesh, blocks, vols
+
+
+def totals(blocks, vols, n, g):
+    act = (slice(g, g + n),) * 3
+    out = np.zeros(5, dtype=np.longdouble)
+    for b, v in zip(blocks, vols):
+        rho = b.f["rho"][act].astype(np.longdouble)
+        out[0] += rho.sum() * v
+        for k, key in enumerate(("vx", "vy", "vz")):
+            out[1 + k] += (rho * b.f[key][act]).sum() * v
+        out[4] += (rho * b.f["etot"][act]).sum() * v
+    return out
+
+
+def run(correct, cycles=3, n=8, g=4):
+    mesh, blocks, vols = smr_blocks(n, g)
+    prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)
+    faces = mesh.face_ints()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    slots = [{0: b.f["rho"], 1: b.f["vx"], 2: b.f["vy"], 3: b.f["vz"], 4: b.f["etot"],
+              9: b.f["pressure"]} for b in blocks]
+    fields = [{q: b.f[k] for q, k in enumerate(O.FC_FIELDS[:5])} for b in blocks]
+    O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+    t0 = totals(blocks, vols, n, g)
+    for _ in range(cycles):
+        dt = min(O.timestep(prm, b) for b in blocks)
+        O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+        fl = [O.step_fc(prm, b, dt) for b in blocks]
+        if correct:
+            O.flux_correct(fields, fl, (n,) * 3, (g,) * 3, faces, cons)
+    t1 = totals(blocks, vols, n, g)
+    return t0, t1
+
+
+def test_smr_run_conserves_with_flux_correction():
+    t0, t1 = run(correct=True)
+    rel = np.abs(t1 - t0) / np.abs(t0)
+    # mass, x/y/z momentum, total energy: round-off only (15 digits or more)
+    assert float(rel.max()) < 1e-15, rel
+    t0u, t1u = run(correct=False)
+    relu = np.abs(t1u - t0u) / np.abs(t0u)
+    assert float(relu[0]) > 1e3 * float(rel[0]), (relu, rel)

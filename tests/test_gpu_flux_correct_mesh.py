@@ -1,0 +1,106 @@
+"""Flux correction at coarse-fine faces on the GPU through the C ABI
+(mhdvlct_flux_correct), against the oracle (its coarsening pinned to the
+reference's own FaceFluxes::coarsen in tests/test_flux_correct_oracle.py):
+
+  - a static-mesh-refinement run -- mesh refresh, step with stored boundary
+    fluxes, flux correction, as the reference's SMR VL decks cycle -- equals
+    the oracle's run bit for bit in FP64 and conserves mass, momentum and
+    total energy to round-off;
+  - the FP32 correction alone equals the oracle's FP32 restatement bit for
+    bit on random fields and fluxes.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from mhdvlct import block as B, capi, mesh as M
+from test_flux_correct_oracle import smr_blocks, totals
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy")
+ONAMES = ("rho", "vx", "vy", "vz", "etot")
+
+
+def test_smr_pipeline_bit_exact_and_conservative():
+    n, g, cycles = 8, 4, 3
+    mesh, oblocks, vols = smr_blocks(n, g)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)
+    blocks = []
+    for ob in oblocks:
+        b = B.Block((n,) * 3, g, ob.widths, mhd=False)
+        b.load_numpy({k: ob.f[o] for k, o in zip(NAMES, ONAMES)})
+        blocks.append(b)
+    bufs = [B.FluxBuffers(b, (0, 1, 2, 3, 4)) for b in blocks]
+    faces, ofaces = mesh.face_array(), mesh.face_ints()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    slots = [{0: b.f["rho"], 1: b.f["vx"], 2: b.f["vy"], 3: b.f["vz"], 4: b.f["etot"],
+              9: b.f["pressure"]} for b in oblocks]
+    fields = [{q: b.f[k] for q, k in enumerate(ONAMES)} for b in oblocks]
+    meth.refresh_faces(blocks, faces, cons)
+    O.refresh_faces(slots, (n,) * 3, (g,) * 3, ofaces, cons)
+    t0 = totals(oblocks, vols, n, g)
+    for _ in range(cycles):
+        dts = [meth.timestep(b) for b in blocks]
+        dt = min(O.timestep(prm, b) for b in oblocks)
+        assert min(dts) == dt
+        meth.refresh_faces(blocks, faces, cons)
+        O.refresh_faces(slots, (n,) * 3, (g,) * 3, ofaces, cons)
+        for b, buf in zip(blocks, bufs):
+            meth.compute_store_fluxes(b, dt, (0, 1, 2, 3, 4), buffers=buf)
+        fl = [O.step_fc(prm, b, dt) for b in oblocks]
+        meth.flux_correct(blocks, bufs, faces, cons)
+        O.flux_correct(fields, fl, (n,) * 3, (g,) * 3, ofaces, cons)
+    torch.cuda.synchronize()
+    for i, (b, ob) in enumerate(zip(blocks, oblocks)):
+        got = b.to_numpy()
+        for k, o in zip(NAMES, ONAMES):
+            assert np.array_equal(got[k], ob.f[o]), (i, k)
+    t1 = totals(oblocks, vols, n, g)
+    assert float((np.abs(t1 - t0) / np.abs(t0)).max()) < 1e-15
+
+
+def test_fp32_correction_bit_exact():
+    n, g = 8, 4
+    mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
+    rng = np.random.default_rng(31)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               dual_energy=True)
+    blocks, bufs, ofields, ofluxes, inputs = [], [], [], [], []
+    m = n + 2 * g
+    for _ in mesh.leaves:
+        st = {"density": 0.5 + rng.random((m, m, m))}
+        for k in ("velocity_x", "velocity_y", "velocity_z", "total_energy",
+                  "internal_energy"):
+            st[k] = rng.standard_normal((m, m, m))
+        st = {k: v.astype(np.float32) for k, v in st.items()}
+        b = B.Block((n,) * 3, g, (1.0, 1.0, 1.0), mhd=False, dual_energy=True,
+                    dtype=torch.float32)
+        b.load_numpy(st)
+        buf = B.FluxBuffers(b, (0, 1, 2, 3, 4, 5))
+        fx = {}
+        for key, t in buf.arrays.items():
+            a = rng.standard_normal(tuple(t.shape)).astype(np.float32)
+            t.copy_(torch.from_numpy(a))
+            fx[key] = a
+        blocks.append(b)
+        bufs.append(buf)
+        ofields.append({q: st[k].copy() for q, k in enumerate(NAMES + ("internal_energy",))})
+        inputs.append(st["density"].copy())
+        ofluxes.append(fx)
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    meth.flux_correct(blocks, bufs, mesh.face_array(), cons)
+    torch.cuda.synchronize()
+    O.flux_correct(ofields, ofluxes, (n,) * 3, (g,) * 3, mesh.face_ints(), cons)
+    changed = 0
+    for i, b in enumerate(blocks):
+        got = b.to_numpy()
+        for q, k in enumerate(NAMES + ("internal_energy",)):
+            assert np.array_equal(got[k], ofields[i][q]), (i, k)
+        changed += int(np.count_nonzero(got["density"] != inputs[i]))
+    # the correction touched the coarse blocks' boundary cells next to the
+    # refined region (7 coarse blocks, 3 corrected faces of 8x8 cells each)
+    assert changed > 0
