@@ -16,6 +16,7 @@
 
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "mhdvlct_gb300.h"
 
@@ -84,6 +85,36 @@ class EnzoMethodMHDVlctGB300 {
     check_(mhdvlct_fill_ghosts_periodic(h_, &b.fields, stream));
   }
 
+  // Method::compute with store_fluxes_for_corrections
+  // (EnzoMethodMHDVlct.cpp:136-141, 250-330): the step also writes the
+  // dt/dx-scaled boundary fluxes into `fc` (Cello's FluxData, on the device).
+  void compute_store_fluxes(Block& b, const MhdFluxCorrection& fc, void* stream = nullptr) {
+    if (!b.is_leaf) return;
+    check_(mhdvlct_block_step_fc(h_, &b.fields, b.dt, &fc, stream));
+  }
+
+  // The ghost refresh of a mesh's leaves whose neighbours may be one level
+  // coarser or finer (Block::refresh_load_field_faces_ with the "linear"
+  // prolongation and restriction), all faces in one launch.
+  void refresh(const std::vector<Block>& blocks, const std::vector<MhdRefreshFace>& faces,
+               unsigned conservative = MHD_CONSERVATIVE_DEFAULT, void* stream = nullptr) {
+    const std::vector<MhdBlockView> v = views_(blocks);
+    check_(mhdvlct_refresh_faces(h_, v.data(), (int)v.size(), faces.data(), (int)faces.size(),
+                                 conservative, stream));
+  }
+
+  // Cello's "flux_correct" Method over the leaves after compute_store_fluxes
+  // (MethodFluxCorrect::compute, src/Cello/problem_MethodFluxCorrect.cpp).
+  void flux_correct(const std::vector<Block>& blocks,
+                    const std::vector<MhdFluxCorrection>& fluxes,
+                    const std::vector<MhdRefreshFace>& faces,
+                    unsigned conservative = MHD_CONSERVATIVE_DEFAULT, void* stream = nullptr) {
+    if (fluxes.size() != blocks.size()) throw Error(MHD_ERR_INVALID, "one flux set per block");
+    const std::vector<MhdBlockView> v = views_(blocks);
+    check_(mhdvlct_flux_correct(h_, v.data(), (int)v.size(), fluxes.data(), faces.data(),
+                                (int)faces.size(), conservative, stream));
+  }
+
   mhdvlct_handle* handle() const noexcept { return h_; }
 
  private:
@@ -96,6 +127,12 @@ class EnzoMethodMHDVlctGB300 {
       throw Error(rc, m);
     }
     h_ = h;
+  }
+  static std::vector<MhdBlockView> views_(const std::vector<Block>& blocks) {
+    std::vector<MhdBlockView> v;
+    v.reserve(blocks.size());
+    for (const Block& b : blocks) v.push_back(b.fields);
+    return v;
   }
   void check_(int rc) const {
     if (rc != MHD_OK) throw Error(rc, mhdvlct_last_error_string(h_));

@@ -4,13 +4,17 @@
 // and (with a GPU) advance one block and compare with a second Method run
 // through the plain C ABI.
 //
-// Usage: method_example            (no GPU needed: construction and errors)
-//        method_example --gpu      (also one timestep + compute on cuda:0)
+// Usage: method_example              (no GPU needed: construction and errors)
+//        method_example --gpu        (also one timestep + compute on cuda:0)
+//        method_example --smr FILE   (a two-level mesh on cuda:0: refresh,
+//                                     step with stored fluxes, flux correction;
+//                                     FILE lists the leaves and refresh faces)
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -27,7 +31,128 @@ static int fail(const char* what) {
   return 1;
 }
 
+static const char* kHydroParams =
+    "Method { mhd_vlct { mhd_choice = \"no_bfield\"; riemann_solver = \"hllc\";"
+    " reconstruct_method = \"plm\"; courant = 0.4; }; }"
+    " Physics { fluid_props { eos { gamma = 1.6666666666666667; }"
+    " floors { density = 1e-200; pressure = 1e-200; } } }";
+
+// Static mesh refinement through the C++ Method: hydro leaves of n^3 cells
+// (ghost depth g) read from `path` (a header "nleaf n g root", one line
+// "level ox oy oz" per leaf with its origin in finest cells, then "nfaces"
+// and one line of 9 ints per refresh face), a moving density contact, two
+// cycles of Cello's order with flux correction; prints the relative change
+// of the mass and total-energy totals.
+static int run_smr(const char* path) {
+  std::ifstream in(path);
+  int nleaf = 0, n = 0, g = 0, root = 0;
+  if (!(in >> nleaf >> n >> g >> root)) return fail("smr header");
+  std::vector<int> level(nleaf), org(3 * (size_t)nleaf);
+  int max_level = 0;
+  for (int i = 0; i < nleaf; i++) {
+    in >> level[i] >> org[3 * i] >> org[3 * i + 1] >> org[3 * i + 2];
+    if (level[i] > max_level) max_level = level[i];
+  }
+  int nfaces = 0;
+  in >> nfaces;
+  std::vector<MhdRefreshFace> faces(nfaces);
+  for (auto& f : faces)
+    in >> f.sender >> f.receiver >> f.type >> f.face[0] >> f.face[1] >> f.face[2] >>
+        f.child[0] >> f.child[1] >> f.child[2];
+  if (!in) return fail("smr file");
+  mhdvlct::EnzoMethodMHDVlctGB300 method(kHydroParams);
+  const int m = n + 2 * g;
+  const size_t M = (size_t)m * m * m, A = (size_t)n * n;
+  const double pi = 3.14159265358979324, gam = 5.0 / 3.0;
+  std::vector<mhdvlct::Block> blocks(nleaf);
+  std::vector<MhdFluxCorrection> fluxes(nleaf);
+  std::vector<void*> owned;
+  std::vector<double> vol(nleaf);
+  auto dev = [&](const std::vector<double>& v) {
+    void* d = nullptr;
+    cudaMalloc(&d, v.size() * sizeof(double));
+    cudaMemcpy(d, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+    owned.push_back(d);
+    return d;
+  };
+  for (int i = 0; i < nleaf; i++) {
+    const double h = 1.0 / (root * n) / (double)(1 << level[i]);
+    const double hf = 1.0 / (root * n) / (double)(1 << max_level);
+    vol[i] = h * h * h;
+    std::vector<double> rho(M), v0(M, 0.4), v1(M, -0.3), v2(M, 0.2), e(M), p(M, 0.0);
+    for (int z = 0; z < m; z++)
+      for (int y = 0; y < m; y++)
+        for (int x = 0; x < m; x++) {
+          const double px = org[3 * i] * hf + (x - g + 0.5) * h;
+          const double py = org[3 * i + 1] * hf + (y - g + 0.5) * h;
+          const double pz = org[3 * i + 2] * hf + (z - g + 0.5) * h;
+          const size_t c = ((size_t)z * m + y) * m + x;
+          rho[c] = 1.0 + 0.5 * std::sin(2 * pi * (px + 2 * py + 3 * pz));
+          e[c] = 0.6 / ((gam - 1.0) * rho[c]) + 0.5 * (0.16 + 0.09 + 0.04);
+        }
+    MhdBlockView& b = blocks[i].fields;
+    std::memset(&b, 0, sizeof(b));
+    b.dtype = MHD_DTYPE_F64;
+    for (int a = 0; a < 3; a++) {
+      b.n[a] = n;
+      b.ghost[a] = g;
+      b.cell_width[a] = h;
+    }
+    b.density = dev(rho);
+    b.velocity[0] = dev(v0);
+    b.velocity[1] = dev(v1);
+    b.velocity[2] = dev(v2);
+    b.total_energy = dev(e);
+    b.pressure = dev(p);
+    std::memset(&fluxes[i], 0, sizeof(fluxes[i]));
+    for (int a = 0; a < 3; a++)
+      for (int sd = 0; sd < 2; sd++)
+        for (int q = 0; q < 5; q++) fluxes[i].flux[a][sd][q] = dev(std::vector<double>(A, 0.0));
+  }
+  auto totals = [&](long double out[2]) {
+    out[0] = out[1] = 0.0L;
+    std::vector<double> r(M), e(M);
+    for (int i = 0; i < nleaf; i++) {
+      cudaMemcpy(r.data(), blocks[i].fields.density, M * sizeof(double), cudaMemcpyDeviceToHost);
+      cudaMemcpy(e.data(), blocks[i].fields.total_energy, M * sizeof(double),
+                 cudaMemcpyDeviceToHost);
+      for (int z = g; z < g + n; z++)
+        for (int y = g; y < g + n; y++)
+          for (int x = g; x < g + n; x++) {
+            const size_t c = ((size_t)z * m + y) * m + x;
+            out[0] += (long double)r[c] * vol[i];
+            out[1] += (long double)r[c] * e[c] * vol[i];
+          }
+    }
+  };
+  method.refresh(blocks, faces);
+  long double t0[2], t1[2];
+  totals(t0);
+  for (int cycle = 0; cycle < 2; cycle++) {
+    double dt = 1e300;
+    for (auto& b : blocks) dt = std::fmin(dt, method.timestep(b));
+    method.refresh(blocks, faces);
+    for (int i = 0; i < nleaf; i++) {
+      blocks[i].dt = dt;
+      method.compute_store_fluxes(blocks[i], fluxes[i]);
+    }
+    method.flux_correct(blocks, fluxes, faces);
+  }
+  totals(t1);
+  for (void* d : owned) cudaFree(d);
+  std::printf("smr ok: mass %.3Le energy %.3Le\n", fabsl(t1[0] - t0[0]) / fabsl(t0[0]),
+              fabsl(t1[1] - t0[1]) / fabsl(t0[1]));
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc > 2 && std::strcmp(argv[1], "--smr") == 0) {
+    try {
+      return run_smr(argv[2]);
+    } catch (const mhdvlct::Error& e) {
+      return fail(e.what());
+    }
+  }
   const bool gpu = argc > 1 && std::strcmp(argv[1], "--gpu") == 0;
   mhdvlct::EnzoMethodMHDVlctGB300 method(kParams);
   if (method.name() != "mhd_vlct") return fail("name");

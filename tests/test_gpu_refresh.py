@@ -38,9 +38,10 @@ def _gpu_blocks(np_blocks, n, g, dtype, mhd, de, npass):
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("cons", [capi.MHD_CONSERVATIVE_DEFAULT, 0])
-def test_two_level_refresh_bit_exact(dtype, cons):
+@pytest.mark.parametrize("n", [(8, 8, 8), (8, 12, 16)])
+def test_two_level_refresh_bit_exact(dtype, cons, n):
     mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
-    n, g = (8, 8, 8), 4
+    g = 4
     npdt = np.float64 if dtype == torch.float64 else np.float32
     ref = mesh_blocks(len(mesh.leaves), n, g, HYDRO_SLOTS, npdt, seed=13)
     blocks = _gpu_blocks(ref, n, g, dtype, mhd=False, de=True, npass=1)

@@ -69,11 +69,12 @@ def _run(blocks, n, g, faces, cons, ref):
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("cons", [capi.MHD_CONSERVATIVE_DEFAULT, 0])
-def test_refresh_matches_reference(dtype, cons):
+@pytest.mark.parametrize("n", [(8, 8, 8), (8, 12, 16)])
+def test_refresh_matches_reference(dtype, cons, n):
     if O.refresh_ref_lib() is None:
         pytest.skip("reference sources not built here")
     mesh = _two_level_mesh()
-    n, g = (8, 8, 8), (4, 4, 4)
+    g = (4, 4, 4)
     faces = mesh.face_ints()
     a = mesh_blocks(len(mesh.leaves), n, g[0], HYDRO_SLOTS, dtype, seed=5, rho_pow2=True)
     b = [{s: x.copy() for s, x in blk.items()} for blk in a]
@@ -112,9 +113,10 @@ def test_general_density_differs_only_by_the_round_trip():
 
 
 @pytest.mark.parametrize("cons", [capi.MHD_CONSERVATIVE_DEFAULT, 0])
-def test_every_ghost_cell_is_written(cons):
+@pytest.mark.parametrize("n", [(8, 8, 8), (8, 12, 16)])
+def test_every_ghost_cell_is_written(cons, n):
     mesh = _two_level_mesh()
-    n, g = (8, 8, 8), (4, 4, 4)
+    g = (4, 4, 4)
     blocks = mesh_blocks(len(mesh.leaves), n, g[0], HYDRO_SLOTS, np.float64, seed=2)
     _run(blocks, n, g, mesh.face_ints(), cons, ref=False)
     for blk in blocks:
