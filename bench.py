@@ -66,6 +66,9 @@ def _args():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--smr-root", type=int, default=8,
                     help="smr mode: root blocks per axis (the central half is refined)")
+    ap.add_argument("--smr-fc", action="store_true",
+                    help="smr mode: store the boundary fluxes and apply the flux "
+                         "correction in every cycle (Method list mhd_vlct, flux_correct)")
     ap.add_argument("--precision-n", type=int, default=512)
     ap.add_argument("--precision-cycles", type=int, default=50)
     ap.add_argument("--tile", type=str, default="",
@@ -533,12 +536,14 @@ def _smr_cpu(n=32, cycles=1):
     return len(obs) * n ** 3 * cycles / el, len(obs)
 
 
-def run_smr(a, root=8, n=32):
+def run_smr(a, root=8, n=32, fc=False):
     """Static mesh refinement, two levels: a periodic root grid of root^3
     blocks of n^3 whose central half along every axis is refined once, hydro
     HLLC + PLM in FP32 with ghost depth 4 (the reference's SMR decks), one
     global dt per cycle; the cycle (dt, mesh refresh with restriction and
-    prolongation, two stages) replayed as one CUDA graph."""
+    prolongation, two stages and, with fc, the flux correction) replayed as
+    one CUDA graph.  The line reports the relative drift of the FP64 mass and
+    total-energy totals over the warm-up and timed cycles."""
     import numpy as np
     import torch
     from mhdvlct import block as B, capi, mesh as M
@@ -573,7 +578,12 @@ def run_smr(a, root=8, n=32):
     farr, nf = mesh.face_array()
     cons = capi.MHD_CONSERVATIVE_DEFAULT
     capi.check(L.mhdvlct_batch_set_refresh_faces(h, farr, nf, cons), meth.handle, "faces")
+    if fc:
+        capi.check(L.mhdvlct_batch_set_flux_correction(h, 0b11111, farr, nf, cons),
+                   meth.handle, "flux correction")
     capi.check(L.mhdvlct_batch_refresh(h, sp), meth.handle, "first refresh")
+    diag0 = (ctypes.c_double * 8)()
+    capi.check(L.mhdvlct_batch_diagnostics(h, diag0, sp), meth.handle, "diag")
     zones = nleaf * n ** 3
     capi.check(L.mhdvlct_batch_run(h, a.warmup, 0, None, sp), meth.handle, "warmup")
     torch.cuda.synchronize()
@@ -613,13 +623,17 @@ def run_smr(a, root=8, n=32):
         cpu = {"value": v_cpu, "unit": "zone-updates/s", "cores": 1, "kind": "port",
                "sample": f"{nb_cpu} leaves of 32^3 (2^3 root grid, one root block "
                          "refined), FP64 oracle, refresh + dt + step, 1 cycle"}
+    drift = {"mass": abs(diag[0] - diag0[0]) / abs(diag0[0]),
+             "total_energy": abs(diag[4] - diag0[4]) / abs(diag0[4]),
+             "cycles": a.warmup + 2 * a.steps}
     return {"mode": "smr", "metric": "zone-updates/s (static mesh refinement, 2 levels)",
+            "flux_correction": fc, "conservation_drift": drift,
             "value": zones * a.steps / (ms / 1e3), "unit": "zone-updates/s",
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
             "dtype": "f32", "data": "synthetic (inclined density contact)",
             "config": {"workload": f"{nleaf} leaves of {n}^3 (+{g} ghosts): {root}^3 root "
                                    f"grid, central {hi - lo}^3 refined once; HLLC+PLM "
-                                   "hydro, global dt",
+                                   "hydro, global dt" + ("; flux correction" if fc else ""),
                        "zones_per_step": zones,
                        "faces": {"same": counts[0], "to_finer": counts[1],
                                  "to_coarser": counts[-1]}},
@@ -822,7 +836,7 @@ def main():
             elif a.mode == "fc":
                 out = run_fc(a)
             elif a.mode == "smr":
-                out = run_smr(a, root=a.smr_root)
+                out = run_smr(a, root=a.smr_root, fc=a.smr_fc)
             else:
                 out = run_precision(a, cycles=a.precision_cycles, N=a.precision_n)
             print(json.dumps(out), flush=True)

@@ -77,6 +77,13 @@ struct mhdvlct_batch {
   char* d_rf = nullptr;
   size_t rf_ptr[2] = {0, 0}, rf_items = 0, rf_chunks = 0;
   int rf_nchunks = -1;  // -1: no face list
+  // flux correction inside the cycle (hydro): every block's stored boundary
+  // fluxes, their per-block FluxOut records, and the correction's plan
+  void* d_flux = nullptr;
+  void* d_fluxout = nullptr;
+  char* d_fcplan = nullptr;
+  FluxCorrectPlan fcplan;
+  bool fc_on = false;
   double* d_dt = nullptr;     // per block
   double* d_dtmin = nullptr;
   double* d_time = nullptr;
@@ -193,6 +200,7 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
         } else {
           B.cur = tmp;
           B.out = next_faces;  // cells in place, faces into the other buffer
+          if (b->fc_on) B.fc = (const char*)b->d_fluxout + (size_t)i * sizeof(FluxOut<R>);
         }
         sb[p][s].push_back(B);
       }
@@ -271,6 +279,8 @@ cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
   info.ty = b->tile_ty[s];
   info.queue = b->d_queue + s;
   info.threads = b->threads[s];
+  info.block_fc = (s == 1 && b->fc_on) ? 1 : 0;
+  info.fc_g = b->g;
   return launch_stage<R>(b->h->solver, sp.recon[s], b->h->de != 0,
                          (const StageBlock<R>*)b->d_sblocks[b->parity][s],
                          b->d_tiles[s], b->ntiles[s], info, b->h->phys, b->grid, st);
@@ -282,6 +292,7 @@ cudaError_t launch_stages(mhdvlct_batch* b, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   for (int s = 0; s < 2; s++)
     if ((e = launch_one_stage<R>(b, s, st)) != cudaSuccess) return e;
+  if (b->fc_on) return launch_flux_correct(b->fcplan, b->d_fcplan, st);
   return cudaSuccess;
 }
 
@@ -441,6 +452,9 @@ extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
   cudaFree(b->d_queue);
   cudaFree(b->d_nbr);
   if (b->d_rf) cudaFree(b->d_rf);
+  cudaFree(b->d_flux);
+  cudaFree(b->d_fluxout);
+  cudaFree(b->d_fcplan);
   cudaFree(b->d_dt);
   cudaFree(b->d_dtmin);
   cudaFree(b->d_time);
@@ -459,6 +473,86 @@ extern "C" int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* v
   if (!b || !v || i < 0 || i >= b->nblocks) return MHD_ERR_INVALID;
   fill_view(b, i, b->parity, v);
   return MHD_OK;
+}
+
+namespace {
+template <class R>
+int set_flux_correction_t(mhdvlct_batch* b, unsigned quantities, const MhdRefreshFace* faces,
+                          int nfaces, unsigned conservative) {
+  const int nx = b->dims[0], ny = b->dims[1], nz = b->dims[2];
+  const size_t face_elems[3] = {(size_t)ny * nz, (size_t)nx * nz, (size_t)nx * ny};
+  int nq = 0;
+  for (int q = 0; q < 6; q++) nq += (quantities >> q) & 1u;
+  const size_t per_block = 2 * (face_elems[0] + face_elems[1] + face_elems[2]) * nq;
+  if (cudaMalloc(&b->d_flux, per_block * b->nblocks * sizeof(R)) != cudaSuccess) {
+    b->d_flux = nullptr;
+    return bfail(b, MHD_ERR_NOMEM, "flux buffers");
+  }
+  std::vector<FluxOut<R>> outs(b->nblocks);
+  std::vector<MhdFluxCorrection> fcs(b->nblocks);
+  std::vector<MhdBlockView> views(b->nblocks);
+  R* p = (R*)b->d_flux;
+  for (int i = 0; i < b->nblocks; i++) {
+    std::memset(&outs[i], 0, sizeof(outs[i]));
+    std::memset(&fcs[i], 0, sizeof(fcs[i]));
+    outs[i].g = b->g;
+    for (int a = 0; a < 3; a++)
+      for (int sd = 0; sd < 2; sd++)
+        for (int q = 0; q < 6; q++)
+          if ((quantities >> q) & 1u) {
+            outs[i].f[a][sd][q] = p;
+            fcs[i].flux[a][sd][q] = p;
+            p += face_elems[a];
+          }
+    fill_view(b, i, 0, &views[i]);  // cell fields: the same for both parities
+  }
+  int rc = plan_flux_correct(b->h, views.data(), b->nblocks, fcs.data(), faces, nfaces,
+                             conservative, b->fcplan);
+  if (rc != MHD_OK) return bfail(b, rc, b->h->err);
+  if (cudaMalloc(&b->d_fluxout, outs.size() * sizeof(FluxOut<R>)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_fcplan, std::max<size_t>(b->fcplan.blob.size(), 16)) !=
+          cudaSuccess)
+    return bfail(b, MHD_ERR_NOMEM, "flux-correction tables");
+  cudaError_t e = cudaMemcpy(b->d_fluxout, outs.data(), outs.size() * sizeof(FluxOut<R>),
+                             cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !b->fcplan.blob.empty())
+    e = cudaMemcpy(b->d_fcplan, b->fcplan.blob.data(), b->fcplan.blob.size(),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  b->fc_on = true;
+  return MHD_OK;
+}
+}  // namespace
+
+extern "C" int mhdvlct_batch_set_flux_correction(mhdvlct_batch* b, unsigned quantities,
+                                                 const MhdRefreshFace* faces, int nfaces,
+                                                 unsigned conservative) {
+  if (!b || quantities >= (1u << 6) || nfaces < 0 || (nfaces > 0 && !faces))
+    return MHD_ERR_INVALID;
+  cudaDeviceSynchronize();
+  b->fc_on = false;
+  cudaFree(b->d_flux);
+  cudaFree(b->d_fluxout);
+  cudaFree(b->d_fcplan);
+  b->d_flux = b->d_fluxout = nullptr;
+  b->d_fcplan = nullptr;
+  b->fcplan = FluxCorrectPlan();
+  if (quantities != 0) {
+    if (b->h->mhd)
+      return bfail(b, MHD_ERR_INVALID,
+                   "Flux corrections are currently only supported in hydro-mode");
+    if (((quantities >> MHD_Q_INTERNAL_ENERGY) & 1u) && !b->h->de)
+      return bfail(b, MHD_ERR_INVALID, "internal_energy fluxes need dual energy");
+    for (int i = 1; i < b->nblocks; i++)
+      for (int a = 0; a < 3; a++)
+        if (b->dims[3 * i + a] != b->dims[a])
+          return bfail(b, MHD_ERR_INVALID, "flux correction needs blocks of equal extents");
+    const int rc = b->dtype == MHD_DTYPE_F64
+                       ? set_flux_correction_t<double>(b, quantities, faces, nfaces, conservative)
+                       : set_flux_correction_t<float>(b, quantities, faces, nfaces, conservative);
+    if (rc != MHD_OK) return rc;
+  }
+  return build_descriptors_any(b, 0);  // the final stage's flux outputs; drops the graphs
 }
 
 extern "C" int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefreshFace* faces,
@@ -705,6 +799,7 @@ int profile_t(mhdvlct_batch* b, int reps, int dt_mode, float* ms, cudaStream_t s
     if (e == cudaSuccess) e = launch_one_stage<R>(b, 0, st);
     cudaEventRecord(ev[3], st);
     if (e == cudaSuccess) e = launch_one_stage<R>(b, 1, st);
+    if (e == cudaSuccess && b->fc_on) e = launch_flux_correct(b->fcplan, b->d_fcplan, st);
     cudaEventRecord(ev[4], st);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
     b->parity ^= 1;

@@ -602,7 +602,10 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     // stage with index 1 (the full-dt stage of vl; never with euler)
     info.gravity = (i == 1 && b->acceleration[0] != nullptr) ? 1 : 0;
     info.npass = np;
-    if (fc && info.final_stage) info.fc = S.d_fc;
+    if (fc && info.final_stage) {
+      info.fc = S.d_fc;
+      info.fc_g = b->ghost[0];
+    }
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, tiles[i],
                         S.ntiles[i], info, h->phys, 0, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");

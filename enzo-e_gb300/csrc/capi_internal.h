@@ -78,4 +78,20 @@ int plan_refresh(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
 cudaError_t launch_refresh_faces(int dtype, const void* d_items, const void* d_chunks,
                                  int nchunks, void* const* d_ptrs, cudaStream_t st);
 
+// Flux correction (fluxcorrect.cu): a validated plan -- the corrected faces,
+// their CTA chunks and the blocks' field and flux pointers in one blob to
+// upload once -- and its launch.
+struct FluxCorrectPlan {
+  std::vector<char> blob;
+  size_t o_chunks = 0, o_blocks = 0;
+  int nchunks = 0;
+  int dtype = MHD_DTYPE_F64;
+  int params[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // kernel parameters
+};
+int plan_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
+                      const MhdFluxCorrection* fluxes, const MhdRefreshFace* faces,
+                      int nfaces, unsigned conservative, FluxCorrectPlan& plan);
+cudaError_t launch_flux_correct(const FluxCorrectPlan& plan, const void* d_blob,
+                                cudaStream_t st);
+
 }  // namespace mhdint

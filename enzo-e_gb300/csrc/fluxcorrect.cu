@@ -164,11 +164,12 @@ __global__ void __launch_bounds__(FC_CHUNK)
 
 }  // namespace
 
-extern "C" int mhdvlct_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
-                                    const MhdFluxCorrection* fluxes,
-                                    const MhdRefreshFace* faces, int nfaces,
-                                    unsigned conservative, void* stream) {
-  if (!h) return MHD_ERR_INVALID;
+namespace mhdint {
+
+int plan_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
+                      const MhdFluxCorrection* fluxes, const MhdRefreshFace* faces,
+                      int nfaces, unsigned conservative, FluxCorrectPlan& plan) {
+  plan = FluxCorrectPlan();
   if (!blocks || !fluxes || nblocks <= 0 || nfaces < 0 || (nfaces > 0 && !faces))
     return fail(h, MHD_ERR_INVALID, "bad flux-correction arguments");
   const MhdBlockView& b0 = blocks[0];
@@ -265,33 +266,55 @@ extern "C" int mhdvlct_flux_correct(mhdvlct_handle* h, const MhdBlockView* block
   for (int k = 0; k < (int)fl.size(); k++)
     for (int s = 0; s < fl[k].ncell; s += FC_CHUNK) chunks.push_back({k, s});
 
-  const size_t o_faces = 0, b_faces = fl.size() * sizeof(FcFace);
-  const size_t o_chunks = (b_faces + 255) / 256 * 256;
-  const size_t o_bp = (o_chunks + chunks.size() * sizeof(FcChunk) + 255) / 256 * 256;
-  const size_t total = o_bp + bp.size() * sizeof(FcBlockPtrs);
+  const size_t b_faces = fl.size() * sizeof(FcFace);
+  plan.o_chunks = (b_faces + 255) / 256 * 256;
+  plan.o_blocks = (plan.o_chunks + chunks.size() * sizeof(FcChunk) + 255) / 256 * 256;
+  plan.blob.assign(plan.o_blocks + bp.size() * sizeof(FcBlockPtrs), 0);
+  memcpy(plan.blob.data(), fl.data(), b_faces);
+  memcpy(plan.blob.data() + plan.o_chunks, chunks.data(), chunks.size() * sizeof(FcChunk));
+  memcpy(plan.blob.data() + plan.o_blocks, bp.data(), bp.size() * sizeof(FcBlockPtrs));
+  plan.nchunks = (int)chunks.size();
+  plan.dtype = b0.dtype;
+  static_assert(sizeof(FcParams) == sizeof(plan.params), "kernel parameters");
+  memcpy(plan.params, &P, sizeof(P));
+  return MHD_OK;
+}
+
+cudaError_t launch_flux_correct(const FluxCorrectPlan& plan, const void* d_blob,
+                                cudaStream_t st) {
+  if (plan.nchunks <= 0) return cudaSuccess;
+  FcParams P;
+  memcpy(&P, plan.params, sizeof(P));
+  const char* dc = (const char*)d_blob;
+  if (plan.dtype == MHD_DTYPE_F64)
+    flux_correct_kernel<double><<<(unsigned)plan.nchunks, FC_CHUNK, 0, st>>>(
+        (const FcFace*)dc, (const FcChunk*)(dc + plan.o_chunks),
+        (const FcBlockPtrs*)(dc + plan.o_blocks), P);
+  else
+    flux_correct_kernel<float><<<(unsigned)plan.nchunks, FC_CHUNK, 0, st>>>(
+        (const FcFace*)dc, (const FcChunk*)(dc + plan.o_chunks),
+        (const FcBlockPtrs*)(dc + plan.o_blocks), P);
+  return cudaGetLastError();
+}
+
+}  // namespace mhdint
+
+extern "C" int mhdvlct_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
+                                    const MhdFluxCorrection* fluxes,
+                                    const MhdRefreshFace* faces, int nfaces,
+                                    unsigned conservative, void* stream) {
+  if (!h) return MHD_ERR_INVALID;
+  FluxCorrectPlan plan;
+  int rc = plan_flux_correct(h, blocks, nblocks, fluxes, faces, nfaces, conservative, plan);
+  if (rc != MHD_OK || plan.nchunks == 0) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   void* d = nullptr;
   // a one-off plan per call: allocate, upload, launch, free after the stream
   // has consumed it
-  cudaError_t e = cudaMallocAsync(&d, total, st);
+  cudaError_t e = cudaMallocAsync(&d, plan.blob.size(), st);
   if (e != cudaSuccess) return fail(h, MHD_ERR_NOMEM, "flux-correction tables");
-  std::vector<char> host(total, 0);
-  memcpy(host.data() + o_faces, fl.data(), b_faces);
-  memcpy(host.data() + o_chunks, chunks.data(), chunks.size() * sizeof(FcChunk));
-  memcpy(host.data() + o_bp, bp.data(), bp.size() * sizeof(FcBlockPtrs));
-  e = cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) {
-    const char* dc = (const char*)d;
-    if (b0.dtype == MHD_DTYPE_F64)
-      flux_correct_kernel<double><<<(unsigned)chunks.size(), FC_CHUNK, 0, st>>>(
-          (const FcFace*)(dc + o_faces), (const FcChunk*)(dc + o_chunks),
-          (const FcBlockPtrs*)(dc + o_bp), P);
-    else
-      flux_correct_kernel<float><<<(unsigned)chunks.size(), FC_CHUNK, 0, st>>>(
-          (const FcFace*)(dc + o_faces), (const FcChunk*)(dc + o_chunks),
-          (const FcBlockPtrs*)(dc + o_bp), P);
-    e = cudaGetLastError();
-  }
+  e = cudaMemcpyAsync(d, plan.blob.data(), plan.blob.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_flux_correct(plan, d, st);
   // the host staging buffer is consumed once the copy has run
   cudaError_t e2 = cudaStreamSynchronize(st);
   cudaFreeAsync(d, st);

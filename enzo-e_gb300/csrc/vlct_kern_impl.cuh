@@ -14,7 +14,8 @@ template <class R, int SOLVER, int RECON, bool DE>
 cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
                       const StageInfo& info, const PhysParams& phys, int grid,
                       cudaStream_t st) {
-  const bool extra = info.fc != nullptr || info.gravity != 0 || info.npass > 0;
+  const bool extra =
+      info.fc != nullptr || info.block_fc != 0 || info.gravity != 0 || info.npass > 0;
   const size_t smem =
       stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty, extra ? info.npass : 0);
   auto k = extra ? stage_kernel<R, SOLVER, RECON, DE, true>

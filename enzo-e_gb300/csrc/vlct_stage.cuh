@@ -430,39 +430,43 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         // final stage writes dt/dx times the flux through the block's active
         // boundary faces.  Every face is written by exactly one tile: the
         // tile (and z-chunk) that owns the cells on its high side.
-        if (EXTRA && info.fc != nullptr && info.final_stage) {
-          const FluxOut<R>* fo = static_cast<const FluxOut<R>*>(info.fc);
-          const int gg = fo->g;
+        if (EXTRA && info.final_stage && (info.fc != nullptr || info.block_fc)) {
+          // only faces on the block's active boundary store: test that first
+          const int gg = info.fc_g;
           const int fpos = d == 0 ? x : (d == 1 ? y : t);
           const int md = d == 0 ? m0 : (d == 1 ? m1 : m2);
           const int side = (fpos == gg - 1) ? 0 : ((fpos == md - gg - 1) ? 1 : -1);
-          const int zc = d == 2 ? t : pl;  // plane of an x or y face
-          bool own;
-          size_t at;
-          if (d == 0) {
-            own = x >= xa - 1 && x < xb - 1 && y >= ya && y < yb && zc >= za && zc < zb &&
-                  inr(y, gg, m1 - gg) && inr(zc, gg, m2 - gg);
-            at = (size_t)(zc - gg) * (m1 - 2 * gg) + (y - gg);
-          } else if (d == 1) {
-            own = y >= ya - 1 && y < yb - 1 && x >= xa && x < xb && zc >= za && zc < zb &&
-                  inr(x, gg, m0 - gg) && inr(zc, gg, m2 - gg);
-            at = (size_t)(zc - gg) * (m0 - 2 * gg) + (x - gg);
-          } else {
-            own = t >= za - 1 && t < zb - 1 && x >= xa && x < xb && y >= ya && y < yb &&
-                  inr(x, gg, m0 - gg) && inr(y, gg, m1 - gg);
-            at = (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg);
-          }
-          if (side >= 0 && own) {
-            const R sc = dtdx[d];
-            const R val[6] = {F.f[L_RHO],
-                              d == 0 ? F.f[L_VI] : (d1 == 0 ? F.f[L_VJ] : F.f[L_VK]),
-                              d == 1 ? F.f[L_VI] : (d1 == 1 ? F.f[L_VJ] : F.f[L_VK]),
-                              d == 2 ? F.f[L_VI] : (d1 == 2 ? F.f[L_VJ] : F.f[L_VK]),
-                              F.f[L_E], F.eflux};
+          if (side >= 0) {
+            const int zc = d == 2 ? t : pl;  // plane of an x or y face
+            bool own;
+            size_t at;
+            if (d == 0) {
+              own = x >= xa - 1 && x < xb - 1 && y >= ya && y < yb && zc >= za && zc < zb &&
+                    inr(y, gg, m1 - gg) && inr(zc, gg, m2 - gg);
+              at = (size_t)(zc - gg) * (m1 - 2 * gg) + (y - gg);
+            } else if (d == 1) {
+              own = y >= ya - 1 && y < yb - 1 && x >= xa && x < xb && zc >= za && zc < zb &&
+                    inr(x, gg, m0 - gg) && inr(zc, gg, m2 - gg);
+              at = (size_t)(zc - gg) * (m0 - 2 * gg) + (x - gg);
+            } else {
+              own = t >= za - 1 && t < zb - 1 && x >= xa && x < xb && y >= ya && y < yb &&
+                    inr(x, gg, m0 - gg) && inr(y, gg, m1 - gg);
+              at = (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg);
+            }
+            if (own) {
+              const FluxOut<R>* fo =
+                  static_cast<const FluxOut<R>*>(B.fc != nullptr ? B.fc : info.fc);
+              const R sc = dtdx[d];
+              const R val[6] = {F.f[L_RHO],
+                                d == 0 ? F.f[L_VI] : (d1 == 0 ? F.f[L_VJ] : F.f[L_VK]),
+                                d == 1 ? F.f[L_VI] : (d1 == 1 ? F.f[L_VJ] : F.f[L_VK]),
+                                d == 2 ? F.f[L_VI] : (d1 == 2 ? F.f[L_VJ] : F.f[L_VK]),
+                                F.f[L_E], F.eflux};
 #pragma unroll
-            for (int q = 0; q < 6; q++) {
-              R* p = fo->f[d][side][q];
-              if (p) p[at] = sc * val[q];
+              for (int q = 0; q < 6; q++) {
+                R* p = fo->f[d][side][q];
+                if (p) p[at] = sc * val[q];
+              }
             }
           }
         }

@@ -30,6 +30,9 @@ template <class R> struct StageBlock {
   const R* pass_cur[4] = {nullptr, nullptr, nullptr, nullptr};
   const R* pass_base[4] = {nullptr, nullptr, nullptr, nullptr};
   R* pass_out[4] = {nullptr, nullptr, nullptr, nullptr};
+  // FluxOut<R> (device) of this block on the final stage when a batch stores
+  // the boundary fluxes for flux correction; null otherwise
+  const void* fc = nullptr;
 };
 
 // One unit of work: a column tile [xa, xb) x [ya, yb) of one block, whose
@@ -62,6 +65,8 @@ struct StageInfo {
   int npass = 0;             // passive scalars advected (0..4)
   const void* fc = nullptr;  // FluxOut<R> (device) on the final stage when the
                              // boundary fluxes are stored; null otherwise
+  int block_fc = 0;          // 1: the blocks carry their own FluxOut (StageBlock::fc)
+  int fc_g = 0;              // ghost depth of the blocks whose fluxes are stored
 };
 
 // Boundary fluxes for flux correction (EnzoMethodMHDVlct.cpp:250-330):

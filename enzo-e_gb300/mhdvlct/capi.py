@@ -34,7 +34,8 @@ EXPORTED = (
     "mhdvlct_refresh_faces", "mhdvlct_refresh_face_box", "mhdvlct_flux_correct",
     "mhdvlct_batch_create", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
-    "mhdvlct_batch_refresh", "mhdvlct_batch_set_refresh_faces", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
+    "mhdvlct_batch_refresh", "mhdvlct_batch_set_refresh_faces",
+    "mhdvlct_batch_set_flux_correction", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
     "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_set_stage_tile",
     "mhdvlct_batch_autotune",
     "mhdvlct_batch_state_region", "mhdvlct_batch_profile",
@@ -155,6 +156,8 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_batch_set_neighbors.argtypes = [vp, P(ip)]
     L.mhdvlct_batch_refresh.argtypes = [vp, vp]
     L.mhdvlct_batch_set_refresh_faces.argtypes = [vp, P(MhdRefreshFace), ip, ctypes.c_uint]
+    L.mhdvlct_batch_set_flux_correction.argtypes = [vp, ctypes.c_uint, P(MhdRefreshFace), ip,
+                                                    ctypes.c_uint]
     L.mhdvlct_batch_step.argtypes = [vp, P(dp), vp]
     L.mhdvlct_batch_timestep.argtypes = [vp, P(dp), vp]
     L.mhdvlct_batch_run.argtypes = [vp, ip, ip, P(dp), vp]

@@ -308,6 +308,14 @@ int mhdvlct_batch_refresh(mhdvlct_batch* b, void* stream);
  * 27-neighbour refresh.  Every block must have the same extents. */
 int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefreshFace* faces,
                                     int nfaces, unsigned conservative);
+/* Store the boundary fluxes of `quantities` (bits of MHD_Q_*) on the final
+ * stage of every cycle and apply the flux correction of the mesh `faces`
+ * (see mhdvlct_flux_correct) right after it, inside the cycle's CUDA graph:
+ * the reference's Method list ["mhd_vlct", "flux_correct"].  Hydro only;
+ * blocks of equal extents.  quantities = 0 turns it off. */
+int mhdvlct_batch_set_flux_correction(mhdvlct_batch* b, unsigned quantities,
+                                      const MhdRefreshFace* faces, int nfaces,
+                                      unsigned conservative);
 /* One VL+CT step of every block; dt_per_block: host array of nblocks. */
 int mhdvlct_batch_step(mhdvlct_batch* b, const double* dt_per_block,
                        void* stream);

@@ -104,3 +104,44 @@ def test_fp32_correction_bit_exact():
     # the correction touched the coarse blocks' boundary cells next to the
     # refined region (7 coarse blocks, 3 corrected faces of 8x8 cells each)
     assert changed > 0
+
+
+def test_batch_graph_with_flux_correction_bit_exact():
+    # the batched form: refresh across levels, the two stages (storing the
+    # boundary fluxes) and the flux correction replayed as one CUDA graph
+    from test_gpu_batch import Batch
+    n, g, cycles = 8, 4, 3
+    mesh, oblocks, vols = smr_blocks(n, g)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)
+    L = capi.lib()
+    bt = Batch(meth, [(n,) * 3] * len(oblocks), [ob.widths for ob in oblocks], ghost=g)
+    for i, ob in enumerate(oblocks):
+        bt.upload(i, {k: ob.f[o] for k, o in zip(NAMES, ONAMES)})
+    farr, nf = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    capi.check(L.mhdvlct_batch_set_refresh_faces(bt.h, farr, nf, cons), meth.handle, "faces")
+    capi.check(L.mhdvlct_batch_set_flux_correction(bt.h, 0b11111, farr, nf, cons),
+               meth.handle, "flux correction")
+    capi.check(L.mhdvlct_batch_refresh(bt.h, None), meth.handle, "refresh")
+    capi.check(L.mhdvlct_batch_run(bt.h, cycles, 0, None, None), meth.handle, "run")
+    # the oracle's run with the correction
+    faces = mesh.face_ints()
+    slots = [{0: b.f["rho"], 1: b.f["vx"], 2: b.f["vy"], 3: b.f["vz"], 4: b.f["etot"],
+              9: b.f["pressure"]} for b in oblocks]
+    fields = [{q: b.f[k] for q, k in enumerate(ONAMES)} for b in oblocks]
+    O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+    for _ in range(cycles):
+        dt = min(O.timestep(prm, b) for b in oblocks)
+        O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+        fl = [O.step_fc(prm, b, dt) for b in oblocks]
+        O.flux_correct(fields, fl, (n,) * 3, (g,) * 3, faces, cons)
+    for i, ob in enumerate(oblocks):
+        got = bt.download(i)
+        for k, o in zip(NAMES, ONAMES):
+            assert np.array_equal(got[k], ob.f[o]), (i, k)
+    # and hydro only, as the reference
+    mhd = B.EnzoMethodMHDVlct()
+    bm = Batch(mhd, [(n,) * 3], [(1.0, 1.0, 1.0)], ghost=g)
+    assert L.mhdvlct_batch_set_flux_correction(bm.h, 1, farr, nf, cons) == capi.MHD_ERR_INVALID
