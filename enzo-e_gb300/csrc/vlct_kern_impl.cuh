@@ -14,12 +14,20 @@ template <class R, int SOLVER, int RECON, bool DE>
 cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
                       const StageInfo& info, const PhysParams& phys, int grid,
                       cudaStream_t st) {
-  const bool extra =
-      info.fc != nullptr || info.block_fc != 0 || info.gravity != 0 || info.npass > 0;
+  const bool all = info.gravity != 0 || info.npass > 0;
+  const bool fc = info.fc != nullptr || info.block_fc != 0;
   const size_t smem =
-      stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty, extra ? info.npass : 0);
-  auto k = extra ? stage_kernel<R, SOLVER, RECON, DE, true>
-                 : stage_kernel<R, SOLVER, RECON, DE, false>;
+      stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty, all ? info.npass : 0);
+  // the flux-storing-only variant exists for the hydro solver (flux
+  // correction is hydro only); the others take the full variant
+  auto k = all ? stage_kernel<R, SOLVER, RECON, DE, EXTRA_ALL>
+               : stage_kernel<R, SOLVER, RECON, DE, EXTRA_NONE>;
+  if (fc && !all) {
+    if constexpr (SOLVER == SOLVER_HLLC)
+      k = stage_kernel<R, SOLVER, RECON, DE, EXTRA_FC>;
+    else
+      k = stage_kernel<R, SOLVER, RECON, DE, EXTRA_ALL>;
+  }
   cudaError_t e = cudaFuncSetAttribute(
       k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -24,9 +24,10 @@
 // them.  The FP64 instantiation is compiled with --fmad=false and matches the
 // reference bit for bit; in the FP32 instantiation the pressure recovery
 // (total minus kinetic minus magnetic energy) and the energy floor / sync run
-// in float-float (vlct_energy.cuh).  A second instantiation (EXTRA) also
-// adds the gravity source, advects passive scalars and stores the boundary
-// fluxes for flux correction; the default one compiles those out.
+// in float-float (vlct_energy.cuh).  Further instantiations (EXTRA) also
+// store the boundary fluxes for flux correction (EXTRA_FC) or, in addition,
+// add the gravity source and advect passive scalars (EXTRA_ALL); the default
+// one compiles all of these out.
 #pragma once
 #include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
@@ -140,10 +141,13 @@ inline int stage_max_threads(int recon) {
                                     : StageBounds<R, RECON_PLM_ATHENA>::threads;
 }
 
-// EXTRA: the instantiation that can also add the gravity source and store
-// the boundary fluxes for flux correction; the default one compiles both out
-// (their run-time checks alone cost ~4% of a stage).
-template <class R, int SOLVER, int RECON, bool DE, bool EXTRA>
+enum { EXTRA_NONE = 0, EXTRA_FC = 1, EXTRA_ALL = 2 };
+
+// EXTRA: EXTRA_NONE compiles the optional work out (its run-time checks alone
+// cost ~4% of a stage); EXTRA_FC can store the boundary fluxes; EXTRA_ALL
+// can also add the gravity source and advect passive scalars (their code
+// paths cost a further ~20% of a stage even when idle).
+template <class R, int SOLVER, int RECON, bool DE, int EXTRA>
 __global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
                                   StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
@@ -155,8 +159,8 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
   SmemLayout Ls;
-  // passive scalars exist only in the EXTRA instantiation
-  const int NP = EXTRA ? info.npass : 0;
+  // passive scalars exist only in the EXTRA_ALL instantiation
+  const int NP = EXTRA == EXTRA_ALL ? info.npass : 0;
   Ls.init(info.tx, info.ty, RP, NRING, NF, NP);
   const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;
   const int PQ = PP * QP;
@@ -430,7 +434,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         // final stage writes dt/dx times the flux through the block's active
         // boundary faces.  Every face is written by exactly one tile: the
         // tile (and z-chunk) that owns the cells on its high side.
-        if (EXTRA && info.final_stage && (info.fc != nullptr || info.block_fc)) {
+        if (EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc)) {
           // only faces on the block's active boundary store: test that first
           const int gg = info.fc_g;
           const int fpos = d == 0 ? x : (d == 1 ? y : t);
@@ -650,7 +654,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           // gravity source on the full-dt stage (EnzoSourceGravity.cpp:17-69,
           // EnzoMHDIntegratorStageCommands.cpp:267-297): start-of-step
           // density and velocity
-          if (EXTRA && info.gravity) {
+          if (EXTRA == EXTRA_ALL && info.gravity) {
             const R dt = s_dt;
             const R rho0 = B.base.c[F_RHO][c];
             const R ax = B.accel[0][c], ay = B.accel[1][c], az = B.accel[2][c];
