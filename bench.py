@@ -13,7 +13,10 @@ stages.  `value` is zone-updates/s of the batched FP32 form with the state
 resident in HBM (the cycle replayed as a CUDA graph); `e2e` is the same
 through the C ABI with the state copied from pinned host memory before and
 back to the host after every step.  Extra keys report the plain per-block
-FP64 path (the Method called block by block) and the batched FP64 form.
+FP64 path (the Method called block by block), the batched FP64 form, a
+serving stream, and a two-level static-mesh-refinement run with flux
+correction (`smr`: 960 hydro leaves of 32^3, the mesh refresh and the
+correction inside the cycle graph, with the drift of the conserved totals).
 
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -66,6 +69,8 @@ def _args():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--smr-root", type=int, default=8,
                     help="smr mode: root blocks per axis (the central half is refined)")
+    ap.add_argument("--no-smr", action="store_true",
+                    help="main mode: skip the static-mesh-refinement key")
     ap.add_argument("--smr-fc", action="store_true",
                     help="smr mode: store the boundary fluxes and apply the flux "
                          "correction in every cycle (Method list mhd_vlct, flux_correct)")
@@ -1010,6 +1015,15 @@ def main():
     if rank == 0 and not a.no_serve:
         serving = run_serve(nreq=a.serve_requests)
 
+    # ---------------------- static mesh refinement, with flux correction
+    smr = None
+    if rank == 0 and not a.no_smr:
+        r = run_smr(a, root=a.smr_root, fc=True)
+        smr = {k: r[k] for k in ("value", "unit", "ms_per_step", "flux_correction",
+                                 "conservation_drift", "kernels_ms_per_step", "refresh",
+                                 "cpu_baseline")}
+        smr["workload"] = r["config"]["workload"]
+
     # ----------------------------------------------------------- CPU baseline
     cpu = None
     if rank == 0 and not a.no_cpu:
@@ -1049,6 +1063,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "serving": serving,
+            "smr": smr,
         }
         line.update(fp64)
         print(json.dumps(line), flush=True)
