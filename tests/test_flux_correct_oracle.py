@@ -38,14 +38,27 @@ def test_coarsen_matches_reference(axis, face):
         assert np.count_nonzero(mine) == (ni // 2) * (no // 2)
 
 
-def smr_blocks(n=8, g=4):
-    """A moving density contact on a 2x2x2 periodic root grid with one root
-    block refined: oracle blocks (hydro) and their cell volumes."""
-    mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
+def three_level_mesh():
+    """A 4^3 periodic root grid, its central 2^3 refined, the centre of that
+    region refined again."""
+    def refine(lvl, c):
+        if lvl == 0:
+            return all(1 <= x < 3 for x in c)
+        return lvl == 1 and all(3 <= x < 5 for x in c)
+    return M.Mesh((4, 4, 4), refine=refine, max_level=2)
+
+
+def smr_blocks(n=8, g=4, mesh=None):
+    """A moving density contact on a periodic mesh (default: a 2x2x2 root
+    grid with one root block refined): oracle blocks (hydro) and their cell
+    volumes."""
+    if mesh is None:
+        mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
+    root = mesh.root[0]
     blocks, vols = [], []
     for i, (lvl, _) in enumerate(mesh.leaves):
-        h = 1.0 / (2 * n) / 2 ** lvl
-        fine = 1.0 / (2 * n) / 2 ** mesh.max_level
+        h = 1.0 / (root * n) / 2 ** lvl
+        fine = 1.0 / (root * n) / 2 ** mesh.max_level
         o = [x * fine for x in mesh.origin(i, (n, n, n))]
         ax = [o[a] + (np.arange(n + 2 * g) - g + 0.5) * h for a in range(3)]
         z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
@@ -73,8 +86,8 @@ def totals(blocks, vols, n, g):
     return out
 
 
-def run(correct, cycles=3, n=8, g=4):
-    mesh, blocks, vols = smr_blocks(n, g)
+def run(correct, cycles=3, n=8, g=4, mesh=None):
+    mesh, blocks, vols = smr_blocks(n, g, mesh)
     prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)
     faces = mesh.face_ints()
     cons = capi.MHD_CONSERVATIVE_DEFAULT
@@ -101,3 +114,11 @@ def test_smr_run_conserves_with_flux_correction():
     t0u, t1u = run(correct=False)
     relu = np.abs(t1u - t0u) / np.abs(t0u)
     assert float(relu[0]) > 1e3 * float(rel[0]), (relu, rel)
+
+
+def test_three_level_run_conserves_with_flux_correction():
+    # level-1 blocks are corrected from their level-2 neighbours and
+    # themselves correct level-0 ones
+    t0, t1 = run(correct=True, cycles=2, mesh=three_level_mesh())
+    rel = np.abs(t1 - t0) / np.abs(t0)
+    assert float(rel.max()) < 1e-15, rel

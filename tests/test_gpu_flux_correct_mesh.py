@@ -23,9 +23,11 @@ NAMES = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy")
 ONAMES = ("rho", "vx", "vy", "vz", "etot")
 
 
-def test_smr_pipeline_bit_exact_and_conservative():
-    n, g, cycles = 8, 4, 3
-    mesh, oblocks, vols = smr_blocks(n, g)
+@pytest.mark.parametrize("levels", [2, 3])
+def test_smr_pipeline_bit_exact_and_conservative(levels):
+    from test_flux_correct_oracle import three_level_mesh
+    n, g, cycles = 8, 4, (3 if levels == 2 else 2)
+    mesh, oblocks, vols = smr_blocks(n, g, three_level_mesh() if levels == 3 else None)
     meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
                                reconstruct_method="plm", courant=0.4)
     prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)

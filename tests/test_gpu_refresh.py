@@ -234,3 +234,23 @@ def test_smr_batch_fp32_close_to_fp64_oracle():
             want = ob.f[ic.ORACLE_NAME[k]][act]
             err = np.abs(got[k][act].astype(np.float64) - want).sum() / np.abs(want).sum()
             assert err <= 1e-5, (i, k, err)
+
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_three_level_refresh_bit_exact(dtype):
+    from test_refresh_oracle import _three_level_mesh
+    mesh = _three_level_mesh()
+    n, g = (8, 8, 8), 4
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    ref = mesh_blocks(len(mesh.leaves), n, g, HYDRO_SLOTS, npdt, seed=17)
+    blocks = _gpu_blocks(ref, n, g, dtype, mhd=False, de=True, npass=1)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc", dual_energy=True)
+    meth.refresh_faces(blocks, mesh.face_array())
+    torch.cuda.synchronize()
+    O.refresh_faces(ref, n, (g,) * 3, mesh.face_ints(), capi.MHD_CONSERVATIVE_DEFAULT)
+    for i, (b, r) in enumerate(zip(blocks, ref)):
+        got = b.to_numpy()
+        for s_, a in r.items():
+            assert np.isfinite(a).all(), (i, SLOT_NAME[s_])
+            assert np.array_equal(got[SLOT_NAME[s_]], a), (i, SLOT_NAME[s_])
