@@ -430,49 +430,60 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           const int pslot = (d == 2) ? (t & 1) : (pl & 1);
           sm[Ls.o_pf + ((d * 2 + pslot) * NP + k) * G + r] = upwind * df;
         }
-        // store_fluxes_for_corrections (EnzoMethodMHDVlct.cpp:250-330): the
-        // final stage writes dt/dx times the flux through the block's active
-        // boundary faces.  Every face is written by exactly one tile: the
-        // tile (and z-chunk) that owns the cells on its high side.
-        if (EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc)) {
-          // only faces on the block's active boundary store: test that first
-          const int gg = info.fc_g;
-          const int fpos = d == 0 ? x : (d == 1 ? y : t);
-          const int md = d == 0 ? m0 : (d == 1 ? m1 : m2);
-          const int side = (fpos == gg - 1) ? 0 : ((fpos == md - gg - 1) ? 1 : -1);
-          if (side >= 0) {
-            const int zc = d == 2 ? t : pl;  // plane of an x or y face
-            bool own;
-            size_t at;
-            if (d == 0) {
-              own = x >= xa - 1 && x < xb - 1 && y >= ya && y < yb && zc >= za && zc < zb &&
-                    inr(y, gg, m1 - gg) && inr(zc, gg, m2 - gg);
-              at = (size_t)(zc - gg) * (m1 - 2 * gg) + (y - gg);
-            } else if (d == 1) {
-              own = y >= ya - 1 && y < yb - 1 && x >= xa && x < xb && zc >= za && zc < zb &&
-                    inr(x, gg, m0 - gg) && inr(zc, gg, m2 - gg);
-              at = (size_t)(zc - gg) * (m0 - 2 * gg) + (x - gg);
-            } else {
-              own = t >= za - 1 && t < zb - 1 && x >= xa && x < xb && y >= ya && y < yb &&
-                    inr(x, gg, m0 - gg) && inr(y, gg, m1 - gg);
-              at = (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg);
-            }
-            if (own) {
-              const FluxOut<R>* fo =
-                  static_cast<const FluxOut<R>*>(B.fc != nullptr ? B.fc : info.fc);
-              const R sc = dtdx[d];
-              const R val[6] = {F.f[L_RHO],
-                                d == 0 ? F.f[L_VI] : (d1 == 0 ? F.f[L_VJ] : F.f[L_VK]),
-                                d == 1 ? F.f[L_VI] : (d1 == 1 ? F.f[L_VJ] : F.f[L_VK]),
-                                d == 2 ? F.f[L_VI] : (d1 == 2 ? F.f[L_VJ] : F.f[L_VK]),
-                                F.f[L_E], F.eflux};
+      }
+    };
+
+    // ---- store_fluxes_for_corrections (EnzoMethodMHDVlct.cpp:250-330): on
+    // the final stage, dt/dx times the fluxes through the block's active
+    // boundary faces, read back from the face fluxes phase B left in shared
+    // memory (valid until phase B overwrites that plane parity two steps
+    // later).  Every face is written by exactly one tile: the tile (and
+    // z-chunk) that owns the cells on its high side.
+    // (the outputs are looked up inside the pass: nothing extra stays live
+    // across the z-march)
+    const bool store_fc =
+        EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc);
+    auto store_fluxes = [&](int t, bool zfaces, int pl) {
+      const FluxOut<R>* fo = static_cast<const FluxOut<R>*>(B.fc != nullptr ? B.fc : info.fc);
+      const int gg = info.fc_g;
+      auto put = [&](int d, int side, size_t at, const R* f) {
+        const R sc = dtdx[d];
 #pragma unroll
-              for (int q = 0; q < 6; q++) {
-                R* p = fo->f[d][side][q];
-                if (p) p[at] = sc * val[q];
-              }
-            }
-          }
+        for (int q = 0; q < 6; q++) {
+          R* p = fo->f[d][side][q];
+          if (!p) continue;
+          const R v = q == 0 ? f[S_RHO * G]
+                    : q <= 3 ? f[(S_MX + q - 1) * G]
+                    : q == 4 ? f[S_E * G] : (DE ? f[S_EINT * G] : R(0));
+          p[at] = sc * v;
+        }
+      };
+      const int xlo = xa > gg ? xa : gg, xhi = xb < m0 - gg ? xb : m0 - gg;
+      const int ylo = ya > gg ? ya : gg, yhi = yb < m1 - gg ? yb : m1 - gg;
+      if (pl >= za && pl < zb && inr(pl, gg, m2 - gg)) {
+        const R* xf = s_xf + (size_t)(pl & 1) * NF * G;
+        const R* yf = s_yf + (size_t)(pl & 1) * NF * G;
+        for (int side = 0; side < 2; side++) {
+          const int x = side == 0 ? gg - 1 : m0 - gg - 1;  // x faces
+          if (x >= xa - 1 && x < xb - 1)
+            for (int y = ylo + tid; y < yhi; y += nthr)
+              put(0, side, (size_t)(pl - gg) * (m1 - 2 * gg) + (y - gg),
+                  xf + (y - hy0) * HP + (x - hx0));
+          const int y = side == 0 ? gg - 1 : m1 - gg - 1;  // y faces
+          if (y >= ya - 1 && y < yb - 1)
+            for (int x2 = xlo + tid; x2 < xhi; x2 += nthr)
+              put(1, side, (size_t)(pl - gg) * (m0 - 2 * gg) + (x2 - gg),
+                  yf + (y - hy0) * HP + (x2 - hx0));
+        }
+      }
+      const int side = t == gg - 1 ? 0 : (t == m2 - gg - 1 ? 1 : -1);  // z faces at t+1/2
+      if (zfaces && side >= 0 && t >= za - 1 && t < zb - 1) {
+        const R* zf = s_zf + (size_t)(t & 1) * NF * G;
+        const int w = xhi - xlo;
+        for (int k = tid; k < w * (yhi - ylo); k += nthr) {
+          const int y = ylo + k / w, x = xlo + k % w;
+          put(2, side, (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg),
+              zf + (y - hy0) * HP + (x - hx0));
         }
       }
     };
@@ -482,11 +493,13 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     __syncthreads();
     phase_b(t0 - 1, false, t0);
     __syncthreads();
+    if (store_fc) store_fluxes(t0 - 1, false, t0);
 
     for (int t = t0; t < zb; t++) {
       // ---- B: z-faces at t+1/2, x/y faces of plane t+1
       phase_b(t, true, t + 1);
       __syncthreads();
+      if (store_fc) store_fluxes(t, true, t + 1);
       // ---- C: edge EMFs (EnzoBfieldMethodCT.cpp:480-590)
       if (MHD) {
         const R* xf0 = s_xf + (size_t)(t & 1) * NF * G;
