@@ -8,7 +8,9 @@
 // planes, the z-face fluxes of two faces, the edge EMFs and the new face B.
 // Per z-plane t the CTA runs four phases separated by __syncthreads():
 //
-//   B  Riemann solves: z-faces at t+1/2, x- and y-faces of plane t+1
+//   B  Riemann solves: z-faces at t+1/2, x- and y-faces of plane t+1 (when
+//      the boundary fluxes are stored, a short pass after B copies the
+//      tile's block-boundary faces out of shared memory)
 //   C  upwinded edge EMFs: E_x, E_y at t+1/2 and E_z of plane t
 //   D1 constrained-transport face updates (Bz at t+1/2, Bx / By of plane t),
 //      and the primitives + cell-centred E of plane t+1+L (L = 1 for NN, 2

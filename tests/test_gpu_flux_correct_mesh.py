@@ -147,3 +147,43 @@ def test_batch_graph_with_flux_correction_bit_exact():
     mhd = B.EnzoMethodMHDVlct()
     bm = Batch(mhd, [(n,) * 3], [(1.0, 1.0, 1.0)], ghost=g)
     assert L.mhdvlct_batch_set_flux_correction(bm.h, 1, farr, nf, cons) == capi.MHD_ERR_INVALID
+
+
+def test_batch_fp32_with_flux_correction_close_to_fp64_oracle():
+    # the benchmarked form: FP32 batch with the correction in the graph, two
+    # cycles against the FP64 oracle (relative L1 over the active cells)
+    from test_gpu_batch import Batch
+    n, g, cycles = 8, 4, 2
+    mesh, oblocks, vols = smr_blocks(n, g)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)
+    L = capi.lib()
+    bt = Batch(meth, [(n,) * 3] * len(oblocks), [ob.widths for ob in oblocks],
+               dtype=capi.MHD_DTYPE_F32, ghost=g)
+    for i, ob in enumerate(oblocks):
+        bt.upload(i, {k: ob.f[o] for k, o in zip(NAMES, ONAMES)})
+    farr, nf = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    capi.check(L.mhdvlct_batch_set_refresh_faces(bt.h, farr, nf, cons), meth.handle, "faces")
+    capi.check(L.mhdvlct_batch_set_flux_correction(bt.h, 0b11111, farr, nf, cons),
+               meth.handle, "flux correction")
+    capi.check(L.mhdvlct_batch_refresh(bt.h, None), meth.handle, "refresh")
+    capi.check(L.mhdvlct_batch_run(bt.h, cycles, 0, None, None), meth.handle, "run")
+    faces = mesh.face_ints()
+    slots = [{0: b.f["rho"], 1: b.f["vx"], 2: b.f["vy"], 3: b.f["vz"], 4: b.f["etot"],
+              9: b.f["pressure"]} for b in oblocks]
+    fields = [{q: b.f[k] for q, k in enumerate(ONAMES)} for b in oblocks]
+    O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+    for _ in range(cycles):
+        dt = min(O.timestep(prm, b) for b in oblocks)
+        O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+        fl = [O.step_fc(prm, b, dt) for b in oblocks]
+        O.flux_correct(fields, fl, (n,) * 3, (g,) * 3, faces, cons)
+    act = (slice(g, g + n),) * 3
+    for i, ob in enumerate(oblocks):
+        got = bt.download(i)
+        for k, o in zip(NAMES, ONAMES):
+            want = ob.f[o][act]
+            err = np.abs(got[k][act].astype(np.float64) - want).sum() / np.abs(want).sum()
+            assert err <= 1e-5, (i, k, err)

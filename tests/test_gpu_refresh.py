@@ -55,11 +55,13 @@ def test_two_level_refresh_bit_exact(dtype, cons, n):
             assert np.array_equal(got[SLOT_NAME[s]], a, equal_nan=True), (i, SLOT_NAME[s])
 
 
-def test_one_level_mhd_refresh_bit_exact():
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_one_level_mhd_refresh_bit_exact(dtype):
     mesh = M.Mesh((2, 1, 2))
     n, g = (8, 12, 6), 3
-    ref = mesh_blocks(len(mesh.leaves), n, g, MHD_SLOTS, np.float64, seed=4)
-    blocks = _gpu_blocks(ref, n, g, torch.float64, mhd=True, de=True, npass=1)
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    ref = mesh_blocks(len(mesh.leaves), n, g, MHD_SLOTS, npdt, seed=4)
+    blocks = _gpu_blocks(ref, n, g, dtype, mhd=True, de=True, npass=1)
     meth = B.EnzoMethodMHDVlct(dual_energy=True)
     meth.refresh_faces(blocks, mesh.faces())
     torch.cuda.synchronize()

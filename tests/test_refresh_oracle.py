@@ -215,6 +215,13 @@ def test_abi_rejects_what_the_reference_asserts_on():
         v2 = view(4)
         v2.n[0] = 16
         assert run([view(4), v2], (0, 1, 0, (1, 0, 0), (0, 0, 0))) == capi.MHD_ERR_INVALID
+        # an empty face list is a no-op (no device work), for the refresh and
+        # for the flux correction
+        arr = (capi.MhdBlockView * 2)(view(4), view(4))
+        assert L.mhdvlct_refresh_faces(h, arr, 2, None, 0, ctypes.c_uint(0), None) == capi.MHD_OK
+        fcs = (capi.MhdFluxCorrection * 2)()
+        assert L.mhdvlct_flux_correct(h, arr, 2, fcs, None, 0, ctypes.c_uint(0),
+                                      None) == capi.MHD_OK
     finally:
         L.mhdvlct_destroy(h)
 
