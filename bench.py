@@ -946,23 +946,28 @@ def main():
                 off += n_
             return off
 
-        copy(False)
-        e2e_steps = max(1, min(a.steps, 5))
+        copy(False)  # the host now holds the current state
+        e2e_steps = max(1, min(a.steps, 10))
+        groups = 8
+        # one warm-up call sets up the copy streams and block groups
+        capi.check(L.mhdvlct_batch_run_host(h32, host.data_ptr(), total, 1, groups, None, sp),
+                   meth.handle, "e2e warm-up")
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        h2d = d2h = 0
         e0.record(stream)
-        for _ in range(e2e_steps):
-            h2d += copy(True)
-            capi.check(L.mhdvlct_batch_run(h32, 1, 0, None, sp), meth.handle, "e2e")
-            d2h += copy(False)
+        # every step: the state in from pinned host memory, one cycle, the new
+        # state back out, the copies pipelined with the full-dt stage
+        capi.check(L.mhdvlct_batch_run_host(h32, host.data_ptr(), total, e2e_steps, groups,
+                                            None, sp), meth.handle, "e2e")
         e1.record(stream)
         torch.cuda.synchronize()
         e_ms = e0.elapsed_time(e1)
         e2e = {"value": world * zones * e2e_steps / (e_ms / 1e3),
-               "unit": "zone-updates/s", "h2d_bytes_per_step": int(h2d // e2e_steps),
-               "d2h_bytes_per_step": int(d2h // e2e_steps), "steps": e2e_steps}
+               "unit": "zone-updates/s", "h2d_bytes_per_step": int(total),
+               "d2h_bytes_per_step": int(total), "steps": e2e_steps,
+               "path": "mhdvlct_batch_run_host, copies pipelined with the full-dt stage "
+                       f"by {groups} block groups"}
     L.mhdvlct_batch_destroy(h32)
 
     # ------------------------------------------- FP64: batched and plain path

@@ -84,6 +84,17 @@ struct mhdvlct_batch {
   char* d_fcplan = nullptr;
   FluxCorrectPlan fcplan;
   bool fc_on = false;
+  // host-state runs (mhdvlct_batch_run_host): the full-dt stage's tiles by
+  // group of consecutive blocks, the groups' block ranges, their queue
+  // counters, and the copy streams and events
+  std::vector<StageTile> h_tiles1;  // host copy of the full-dt stage's tiles
+  int hg_n = 0;
+  std::vector<int> hg_first;        // first block of each group (+ end)
+  StageTile* d_gtiles = nullptr;
+  std::vector<int> hg_tile0, hg_ntile;
+  int* d_gqueue = nullptr;
+  cudaStream_t s_d2h = nullptr, s_h2d = nullptr;
+  std::vector<cudaEvent_t> ev;      // 3 per group: stage done, out, in
   double* d_dt = nullptr;     // per block
   double* d_dtmin = nullptr;
   double* d_time = nullptr;
@@ -232,6 +243,7 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
                         const std::pair<double, StageTile>& c) { return a.first > c.first; });
     for (auto& o : order[s]) tiles[s].push_back(o.second);
     b->ntiles[s] = (int)tiles[s].size();
+    if (s == 1) b->h_tiles1 = tiles[s];
     b->tile_tx[s] = tx[s];
     b->tile_ty[s] = ty[s];
   }
@@ -259,6 +271,7 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
       return rc;
   cudaStreamSynchronize(st);
   drop_graphs(b);
+  b->hg_n = 0;  // the host-run groups are rebuilt from the new tiles
   return MHD_OK;
 }
 
@@ -455,6 +468,11 @@ extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
   cudaFree(b->d_flux);
   cudaFree(b->d_fluxout);
   cudaFree(b->d_fcplan);
+  cudaFree(b->d_gtiles);
+  cudaFree(b->d_gqueue);
+  for (cudaEvent_t x : b->ev) cudaEventDestroy(x);
+  if (b->s_d2h) cudaStreamDestroy(b->s_d2h);
+  if (b->s_h2d) cudaStreamDestroy(b->s_h2d);
   cudaFree(b->d_dt);
   cudaFree(b->d_dtmin);
   cudaFree(b->d_time);
@@ -752,6 +770,203 @@ extern "C" int mhdvlct_batch_set_stage_tile(mhdvlct_batch* b, int stage, int til
   }
   b->threads[stage] = threads ? threads : 256;
   return build_descriptors_any(b, 0);
+}
+
+namespace {
+
+// Groups of consecutive blocks of about equal zone counts, and the full-dt
+// stage's tiles of each group (in the batch's largest-first order).
+int setup_host_groups(mhdvlct_batch* b, int ngroups) {
+  if (b->hg_n == ngroups) return MHD_OK;
+  long total = 0;
+  std::vector<long> zones(b->nblocks);
+  for (int i = 0; i < b->nblocks; i++) {
+    zones[i] = (long)b->dims[3 * i] * b->dims[3 * i + 1] * b->dims[3 * i + 2];
+    total += zones[i];
+  }
+  b->hg_first.assign(1, 0);
+  long acc = 0;
+  for (int i = 0; i < b->nblocks; i++) {
+    acc += zones[i];
+    const int k = (int)b->hg_first.size();  // the group being filled
+    if (k < ngroups && acc * ngroups >= total * k && i + 1 < b->nblocks)
+      b->hg_first.push_back(i + 1);
+  }
+  b->hg_first.push_back(b->nblocks);
+  const int ng = (int)b->hg_first.size() - 1;
+  std::vector<int> group_of(b->nblocks);
+  for (int g = 0; g < ng; g++)
+    for (int i = b->hg_first[g]; i < b->hg_first[g + 1]; i++) group_of[i] = g;
+  std::vector<StageTile> sorted;
+  b->hg_tile0.assign(ng, 0);
+  b->hg_ntile.assign(ng, 0);
+  for (int g = 0; g < ng; g++) {
+    b->hg_tile0[g] = (int)sorted.size();
+    for (const StageTile& t : b->h_tiles1)
+      if (group_of[t.block] == g) sorted.push_back(t);
+    b->hg_ntile[g] = (int)sorted.size() - b->hg_tile0[g];
+  }
+  cudaFree(b->d_gtiles);
+  cudaFree(b->d_gqueue);
+  b->d_gtiles = nullptr;
+  b->d_gqueue = nullptr;
+  if (cudaMalloc((void**)&b->d_gtiles, std::max<size_t>(1, sorted.size()) * sizeof(StageTile)) !=
+          cudaSuccess ||
+      cudaMalloc((void**)&b->d_gqueue, ng * sizeof(int)) != cudaSuccess)
+    return bfail(b, MHD_ERR_NOMEM, "host-run tables");
+  cudaError_t e = cudaMemcpy(b->d_gtiles, sorted.data(), sorted.size() * sizeof(StageTile),
+                             cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  if (!b->s_d2h && cudaStreamCreateWithFlags(&b->s_d2h, cudaStreamNonBlocking) != cudaSuccess)
+    return bfail(b, MHD_ERR_CUDA, "copy stream");
+  if (!b->s_h2d && cudaStreamCreateWithFlags(&b->s_h2d, cudaStreamNonBlocking) != cudaSuccess)
+    return bfail(b, MHD_ERR_CUDA, "copy stream");
+  while ((int)b->ev.size() < 3 * ng + 1) {
+    cudaEvent_t x;
+    if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess)
+      return bfail(b, MHD_ERR_CUDA, "events");
+    b->ev.push_back(x);
+  }
+  b->hg_n = ng;
+  return MHD_OK;
+}
+
+// The state bytes of group g: its cells and its current face B, as offsets
+// in the pool and in the host buffer (cells of all blocks, then the current
+// faces of all blocks).
+struct GroupSpan {
+  size_t dev[2], host[2], bytes[2];
+  int n;
+};
+GroupSpan group_span(const mhdvlct_batch* b, int g, int parity, size_t esz) {
+  GroupSpan sp{};
+  const int i0 = b->hg_first[g], i1 = b->hg_first[g + 1];
+  // cells: from the first field of block i0 to the first field of block i1
+  auto first_cell = [&](int i) -> size_t {
+    if (i >= b->nblocks) return b->cells_elems;
+    size_t lo = (size_t)-1;
+    for (int k = 0; k < NCELL; k++)
+      if (b->off[i].ext[k] != (size_t)-1) lo = std::min(lo, b->off[i].ext[k]);
+    return lo;
+  };
+  const size_t c0 = first_cell(i0), c1 = first_cell(i1);
+  sp.dev[0] = c0 * esz;
+  sp.host[0] = c0 * esz;
+  sp.bytes[0] = (c1 - c0) * esz;
+  sp.n = 1;
+  if (b->h->mhd) {
+    const size_t base = parity == 0 ? b->cells_elems : b->fa_end;
+    const size_t end = parity == 0 ? b->fa_end : b->state_elems;
+    auto first_face = [&](int i) -> size_t {
+      if (i >= b->nblocks) return end;
+      return parity == 0 ? b->off[i].fa[0] : b->off[i].fb[0];
+    };
+    const size_t f0 = first_face(i0), f1 = first_face(i1);
+    sp.dev[1] = f0 * esz;
+    sp.host[1] = (b->cells_elems + (f0 - base)) * esz;
+    sp.bytes[1] = (f1 - f0) * esz;
+    sp.n = 2;
+  }
+  return sp;
+}
+
+template <class R>
+int run_host_t(mhdvlct_batch* b, char* host, int ncycles, cudaStream_t st) {
+  const size_t esz = sizeof(R);
+  char* dev = (char*)b->pool;
+  const int ng = b->hg_n;
+  cudaError_t e = cudaSuccess;
+  auto copy = [&](const GroupSpan& sp, bool in, cudaStream_t cs) {
+    for (int k = 0; k < sp.n && e == cudaSuccess; k++)
+      e = in ? cudaMemcpyAsync(dev + sp.dev[k], host + sp.host[k], sp.bytes[k],
+                               cudaMemcpyHostToDevice, cs)
+             : cudaMemcpyAsync(host + sp.host[k], dev + sp.dev[k], sp.bytes[k],
+                               cudaMemcpyDeviceToHost, cs);
+  };
+  cudaEvent_t* ev = b->ev.data();  // [0, ng): stage done; [ng, 2ng): out; [2ng, 3ng): in
+  cudaEvent_t start = ev[3 * ng];
+  e = cudaMemsetAsync(b->d_time, 0, sizeof(double), st);
+  // the first cycle's input, on the compute stream
+  for (int g = 0; g < ng && e == cudaSuccess; g++) copy(group_span(b, g, b->parity, esz), true, st);
+  for (int c = 0; c < ncycles && e == cudaSuccess; c++) {
+    if (c > 0)  // the input of this cycle: every group's copy back in
+      for (int g = 0; g < ng && e == cudaSuccess; g++)
+        e = cudaStreamWaitEvent(st, ev[2 * ng + g], 0);
+    if (e == cudaSuccess) e = launch_timestep_b<R>(b, 1, st);
+    if (e == cudaSuccess) {
+      add_scalar_kernel<<<1, 1, 0, st>>>(b->d_time, b->d_dtmin);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = launch_refresh_b<R>(b, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_gqueue, 0, ng * sizeof(int), st);
+    if (e == cudaSuccess) e = launch_one_stage<R>(b, 0, st);
+    const StagePlan sp = stage_plan(b->h);
+    for (int g = 0; g < ng && e == cudaSuccess; g++) {
+      StageInfo info;
+      info.s = sp.s[1];
+      info.S = sp.S[1];
+      info.final_stage = 1;
+      info.dt_factor = sp.dt_factor[1];
+      info.tx = b->tile_tx[1];
+      info.ty = b->tile_ty[1];
+      info.queue = b->d_gqueue + g;
+      info.threads = b->threads[1];
+      info.block_fc = b->fc_on ? 1 : 0;
+      info.fc_g = b->g;
+      e = launch_stage<R>(b->h->solver, sp.recon[1], b->h->de != 0,
+                          (const StageBlock<R>*)b->d_sblocks[b->parity][1],
+                          b->d_gtiles + b->hg_tile0[g], b->hg_ntile[g], info, b->h->phys,
+                          b->grid, st);
+      if (e == cudaSuccess && !b->fc_on) e = cudaEventRecord(ev[g], st);
+    }
+    if (e == cudaSuccess && b->fc_on) {
+      // the correction needs every block's fluxes: the groups leave after it
+      e = launch_flux_correct(b->fcplan, b->d_fcplan, st);
+      for (int g = 0; g < ng && e == cudaSuccess; g++) e = cudaEventRecord(ev[g], st);
+    }
+    b->parity ^= 1;  // the new face B is in the other buffer
+    const bool more = c + 1 < ncycles;
+    for (int g = 0; g < ng && e == cudaSuccess; g++) {
+      const GroupSpan sp_g = group_span(b, g, b->parity, esz);
+      e = cudaStreamWaitEvent(b->s_d2h, ev[g], 0);
+      if (e == cudaSuccess) copy(sp_g, false, b->s_d2h);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[ng + g], b->s_d2h);
+      if (more && e == cudaSuccess) {
+        // the next cycle's input: this group's state, back from the host
+        e = cudaStreamWaitEvent(b->s_h2d, ev[ng + g], 0);
+        if (e == cudaSuccess) copy(sp_g, true, b->s_h2d);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2 * ng + g], b->s_h2d);
+      }
+    }
+  }
+  // the call's stream completes once the last state is on the host
+  for (int g = 0; g < ng && e == cudaSuccess; g++) e = cudaStreamWaitEvent(st, ev[ng + g], 0);
+  (void)start;
+  if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" int mhdvlct_batch_run_host(mhdvlct_batch* b, void* host, size_t bytes, int ncycles,
+                                      int ngroups, double* elapsed_out, void* stream) {
+  if (!b || !host || ncycles < 0 || ngroups < 1) return MHD_ERR_INVALID;
+  const size_t esz = b->dtype == MHD_DTYPE_F64 ? 8 : 4;
+  const size_t need = (b->h->mhd ? b->fa_end : b->cells_elems) * esz;
+  if (bytes < need) return bfail(b, MHD_ERR_INVALID, "host buffer smaller than the state");
+  if (int rc = setup_host_groups(b, std::min(ngroups, b->nblocks))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int rc = b->dtype == MHD_DTYPE_F64 ? run_host_t<double>(b, (char*)host, ncycles, st)
+                                           : run_host_t<float>(b, (char*)host, ncycles, st);
+  if (rc != MHD_OK) return rc;
+  if (elapsed_out) {
+    cudaError_t e = cudaMemcpyAsync(elapsed_out, b->d_time, sizeof(double),
+                                    cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return MHD_OK;
 }
 
 extern "C" int mhdvlct_batch_state_segments(mhdvlct_batch* b, void** dev_ptrs,

@@ -39,7 +39,7 @@ EXPORTED = (
     "mhdvlct_batch_run", "mhdvlct_batch_set_tile", "mhdvlct_batch_set_stage_tile",
     "mhdvlct_batch_autotune",
     "mhdvlct_batch_state_region", "mhdvlct_batch_profile",
-    "mhdvlct_batch_diagnostics", "mhdvlct_batch_state_segments", "mhdserve_create",
+    "mhdvlct_batch_diagnostics", "mhdvlct_batch_state_segments", "mhdvlct_batch_run_host", "mhdserve_create",
     "mhdserve_destroy", "mhdserve_submit", "mhdserve_pump", "mhdserve_poll",
     "mhdserve_result", "mhdserve_timing", "mhdserve_last_error_string",
 )
@@ -168,6 +168,7 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_batch_set_stage_tile.argtypes = [vp, ip, ip, ip, ip, ip]
     L.mhdvlct_batch_diagnostics.argtypes = [vp, P(dp), vp]
     L.mhdvlct_batch_state_segments.argtypes = [vp, P(vp), P(ctypes.c_size_t), ip, P(ip)]
+    L.mhdvlct_batch_run_host.argtypes = [vp, vp, ctypes.c_size_t, ip, ip, P(dp), vp]
     L.mhdserve_create.argtypes = [P(MhdVlctParams), ctypes.c_size_t, ip, P(vp)]
     L.mhdserve_destroy.argtypes = [vp]
     L.mhdserve_submit.argtypes = [vp, P(MhdServeRequest), P(ip)]

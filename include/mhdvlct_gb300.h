@@ -358,6 +358,18 @@ int mhdvlct_batch_diagnostics(mhdvlct_batch* b, double* out, void* stream);
  * buffer), as one or two contiguous device segments: dev_ptrs[i] / bytes[i]
  * for i < *nsegments (max_segments >= 2).  Valid until the next step; what a
  * host that keeps the fields transfers each cycle. */
+/* Advance ncycles with the state held in pinned host memory: `host` holds
+ * every block's cell fields, then every block's current face B, back to back
+ * (the segments of mhdvlct_batch_state_segments, `bytes` their total).  Every
+ * cycle copies the state in, runs the cycle with one global dt and copies
+ * the new state back out -- Cello's host-resident field data.  The copies
+ * are pipelined with the full-dt stage by `ngroups` groups of consecutive
+ * blocks: a group's new state leaves as soon as its stage is done and, when
+ * another cycle follows, comes straight back in while later groups still
+ * compute.  The stream completes when the final state is in `host`;
+ * elapsed_out (may be NULL) receives the simulated time advanced. */
+int mhdvlct_batch_run_host(mhdvlct_batch* b, void* host, size_t bytes, int ncycles,
+                           int ngroups, double* elapsed_out, void* stream);
 int mhdvlct_batch_state_segments(mhdvlct_batch* b, void** dev_ptrs, size_t* bytes,
                                  int max_segments, int* nsegments);
 /* Run `reps` cycles as individual launches with CUDA events between the

@@ -87,20 +87,26 @@ class Batch:
 _cudart = None
 
 
+def _load_cudart():
+    """The CUDA runtime the library itself loaded."""
+    capi.lib()
+    path = None
+    with open("/proc/self/maps") as f:
+        for line in f:
+            if "libcudart" in line:
+                path = line.split()[-1]
+                break
+    rt = ctypes.CDLL(path or "libcudart.so")
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    rt.cudaMemset.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t]
+    return rt
+
+
 def ctypes_cuda_memcpy(dev_ptr, host_arr, to_device):
     """cudaMemcpy through the CUDA runtime the library itself loaded."""
     global _cudart
     if _cudart is None:
-        capi.lib()
-        path = None
-        with open("/proc/self/maps") as f:
-            for line in f:
-                if "libcudart" in line:
-                    path = line.split()[-1]
-                    break
-        _cudart = ctypes.CDLL(path or "libcudart.so")
-        _cudart.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
-                                       ctypes.c_size_t, ctypes.c_int]
+        _cudart = _load_cudart()
     n = host_arr.nbytes
     if to_device:
         rc = _cudart.cudaMemcpy(dev_ptr, host_arr.ctypes.data, n, 1)
@@ -303,3 +309,68 @@ def test_zchunked_default_tiles_bit_exact():
     act = (slice(g, g + n[2]), slice(g, g + n[1]), slice(g, g + n[0]))
     for k in KEYS[:8]:
         assert np.array_equal(got[k][act], ob.f[ic.ORACLE_NAME[k]][act]), k
+
+
+@pytest.mark.parametrize("ngroups", [1, 3, 8])
+def test_run_host_matches_device_run(ngroups):
+    """mhdvlct_batch_run_host (state in pinned host memory, copies pipelined
+    with the full-dt stage by block groups) gives the same state, bit for
+    bit, as the device-resident graph run of the same cycles."""
+    meth = B.EnzoMethodMHDVlct()
+    nb, N = 2, 24
+    blocks, w = ic.turbulent_box(N=N, nb=nb, g=3, seed=5, mach=1.5)
+    nbr = ic.brick_neighbors(nb)
+    L = capi.lib()
+    runs = []
+    for _ in range(2):
+        bt = Batch(meth, [(12, 12, 12)] * 8, [w] * 8, dtype=capi.MHD_DTYPE_F32)
+        capi.check(L.mhdvlct_batch_set_neighbors(
+            bt.h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())))
+        for i, s in enumerate(blocks):
+            bt.upload(i, s)
+        runs.append(bt)
+    dev, hst = runs
+    t_dev, t_host = ctypes.c_double(), ctypes.c_double()
+    capi.check(L.mhdvlct_batch_run(dev.h, 3, 0, ctypes.byref(t_dev), None), meth.handle, "run")
+    # the host buffer: the current state segments back to back
+    segp = (ctypes.c_void_p * 2)()
+    segb = (ctypes.c_size_t * 2)()
+    nseg = ctypes.c_int()
+    capi.check(L.mhdvlct_batch_state_segments(hst.h, segp, segb, 2, ctypes.byref(nseg)))
+    total = sum(segb[k] for k in range(nseg.value))
+    host = torch.empty(total, dtype=torch.uint8, pin_memory=True)
+    off = 0
+    for k in range(nseg.value):
+        ctypes_cuda_memcpy_raw(host.data_ptr() + off, segp[k], segb[k], to_device=False)
+        off += segb[k]
+    # scramble the device copy: the run must take its input from the host
+    for k in range(nseg.value):
+        torch.cuda.synchronize()
+        _memset(segp[k], segb[k])
+    capi.check(L.mhdvlct_batch_run_host(hst.h, host.data_ptr(), total, 3, ngroups,
+                                        ctypes.byref(t_host), None), meth.handle, "run_host")
+    assert t_host.value == t_dev.value
+    torch.cuda.synchronize()
+    # the device run's state, in the same layout
+    capi.check(L.mhdvlct_batch_state_segments(dev.h, segp, segb, 2, ctypes.byref(nseg)))
+    want = torch.empty(total, dtype=torch.uint8, pin_memory=True)
+    off = 0
+    for k in range(nseg.value):
+        ctypes_cuda_memcpy_raw(want.data_ptr() + off, segp[k], segb[k], to_device=False)
+        off += segb[k]
+    assert torch.equal(host, want)
+
+
+def ctypes_cuda_memcpy_raw(dst, src, nbytes, to_device):
+    global _cudart
+    if _cudart is None:
+        _cudart = _load_cudart()
+    kind = 1 if to_device else 2
+    assert _cudart.cudaMemcpy(dst, src, nbytes, kind) == 0
+
+
+def _memset(ptr, nbytes):
+    global _cudart
+    if _cudart is None:
+        _cudart = _load_cudart()
+    assert _cudart.cudaMemset(ptr, 0x7F, nbytes) == 0
