@@ -821,7 +821,7 @@ int setup_host_groups(mhdvlct_batch* b, int ngroups) {
     return bfail(b, MHD_ERR_CUDA, "copy stream");
   if (!b->s_h2d && cudaStreamCreateWithFlags(&b->s_h2d, cudaStreamNonBlocking) != cudaSuccess)
     return bfail(b, MHD_ERR_CUDA, "copy stream");
-  while ((int)b->ev.size() < 3 * ng + 1) {
+  while ((int)b->ev.size() < 3 * ng) {
     cudaEvent_t x;
     if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess)
       return bfail(b, MHD_ERR_CUDA, "events");
@@ -884,7 +884,6 @@ int run_host_t(mhdvlct_batch* b, char* host, int ncycles, cudaStream_t st) {
                                cudaMemcpyDeviceToHost, cs);
   };
   cudaEvent_t* ev = b->ev.data();  // [0, ng): stage done; [ng, 2ng): out; [2ng, 3ng): in
-  cudaEvent_t start = ev[3 * ng];
   e = cudaMemsetAsync(b->d_time, 0, sizeof(double), st);
   // the first cycle's input, on the compute stream
   for (int g = 0; g < ng && e == cudaSuccess; g++) copy(group_span(b, g, b->parity, esz), true, st);
@@ -942,7 +941,6 @@ int run_host_t(mhdvlct_batch* b, char* host, int ncycles, cudaStream_t st) {
   }
   // the call's stream completes once the last state is on the host
   for (int g = 0; g < ng && e == cudaSuccess; g++) e = cudaStreamWaitEvent(st, ev[ng + g], 0);
-  (void)start;
   if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
   return MHD_OK;
 }
