@@ -309,13 +309,29 @@ cudaError_t launch_stages(mhdvlct_batch* b, cudaStream_t st) {
   return cudaSuccess;
 }
 
+// 256-thread CTAs that fill the GPU about four times over (SM count of the
+// current device, thread-safe one-time initialisation)
+size_t fill_ctas() {
+  static const size_t n = [] {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        nsm <= 0)
+      nsm = 1;
+    return (size_t)nsm * 8 * 4;
+  }();
+  return n;
+}
+
 template <class R>
 cudaError_t launch_timestep_b(mhdvlct_batch* b, int global_min, cudaStream_t st) {
-  // chunks per block so that the grid covers the GPU a few times over
+  // chunks per block so that the grid covers the GPU a few times over, also
+  // when there are few blocks (a single large serving request)
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
-  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 2048, 64));
+  const int cpb = (int)std::max<size_t>(
+      1, std::min<size_t>(per / 2048, std::max<size_t>(64, fill_ctas() / b->nblocks)));
   return launch_timestep<R>(b->h->mhd != 0, b->h->de != 0,
                             (const AuxBlock<R>*)b->d_aux[b->parity], b->nblocks, cpb,
                             b->h->phys, b->d_smax, b->h->params.courant, global_min,
@@ -331,7 +347,8 @@ cudaError_t launch_refresh_b(mhdvlct_batch* b, cudaStream_t st) {
   size_t cells = 0;
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
-  const int cpb = (int)std::max<size_t>(1, std::min<size_t>(per / 4096, 32));
+  const int cpb = (int)std::max<size_t>(
+      1, std::min<size_t>(per / 4096, std::max<size_t>(32, fill_ctas() / b->nblocks)));
   int max_m = 0;
   for (auto& o : b->off) max_m = std::max(max_m, std::max(o.m[0], std::max(o.m[1], o.m[2])));
   return launch_refresh<R>((const AuxBlock<R>*)b->d_aux[b->parity], b->d_nbr,
