@@ -49,12 +49,12 @@ def test_admission_budget_and_rejection():
     ts = [srv.submit(s, 16, 3, "hlld", "plm", box) for _ in range(5)]
     srv.drain(ts)
     assert all(srv.poll(t) == DONE for t in ts)
-    # admission never exceeded the budget: at most two ran concurrently
+    # admission never exceeded the budget: at most two ran at any instant
+    # (checked at every admission, where the running count can rise)
     spans = [srv.timing(t) for t in ts]
-    for i, (_, a_i, d_i) in enumerate(spans):
-        overlap = sum(1 for j, (_, a_j, d_j) in enumerate(spans)
-                      if j != i and a_j < d_i and a_i < d_j)
-        assert overlap <= 1
+    for _, a_i, _ in spans:
+        running = sum(1 for _, a_j, d_j in spans if a_j <= a_i < d_j)
+        assert running <= 2
     big, bbox = _req(64, 4, 1.0, "hlld")
     with pytest.raises(capi.MhdError):
         srv.submit(big, 64, 2, "hlld", "plm", bbox)
