@@ -48,6 +48,8 @@ struct mhdvlct_batch {
   int dtype = MHD_DTYPE_F32;
   int nblocks = 0;
   int g = 3;
+  int npass = 0;    // passive scalars of every block (0..4)
+  int gravity = 0;  // 1: every block carries acceleration_x/y/z
   std::vector<int> dims;       // 3 per block (active)
   std::vector<double> widths;  // 3 per block
   void* pool = nullptr;
@@ -59,6 +61,8 @@ struct mhdvlct_batch {
   // element offsets (in units of the real type) of every array of block i
   struct Off {
     size_t ext[NCELL], tmp[NCELL], fa[3], fb[3], tf[3], pres;
+    size_t pas[4], ptmp[4], acc[3];  // passive scalars (state, half step),
+                                     // acceleration; (size_t)-1 when absent
     int m[3];
   };
   std::vector<Off> off;
@@ -205,6 +209,15 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
         }
         B.dt = b->d_dt + i;
         B.base = cur_faces;
+        for (int d = 0; d < 3; d++) B.accel[d] = b->gravity ? b->ptr<R>(O.acc[d]) : nullptr;
+        for (int k = 0; k < b->npass; k++) {
+          // half dt: state -> half step; full dt: half step -> state
+          R* ep = b->ptr<R>(O.pas[k]);
+          R* tp = b->ptr<R>(O.ptmp[k]);
+          B.pass_base[k] = ep;
+          B.pass_cur[k] = s == 0 ? ep : tp;
+          B.pass_out[k] = s == 0 ? tp : ep;
+        }
         if (s == 0) {
           B.cur = cur_faces;
           B.out = tmp;
@@ -222,6 +235,8 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
       }
       A.f = cur_faces;
       A.pressure = b->ptr<R>(O.pres);
+      for (int k = 0; k < b->npass; k++) A.pass[k] = b->ptr<R>(O.pas[k]);
+      for (int d = 0; d < 3; d++) A.accel[d] = b->gravity ? b->ptr<R>(O.acc[d]) : nullptr;
       aux[p].push_back(A);
     }
     const TileChoice c = choice_for(b, i);
@@ -294,6 +309,10 @@ cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
   info.threads = b->threads[s];
   info.block_fc = (s == 1 && b->fc_on) ? 1 : 0;
   info.fc_g = b->g;
+  // the gravity source enters the full-dt stage only
+  // (EnzoMHDIntegratorStageCommands.cpp:279)
+  info.gravity = s == 1 ? b->gravity : 0;
+  info.npass = b->npass;
   return launch_stage<R>(b->h->solver, sp.recon[s], b->h->de != 0,
                          (const StageBlock<R>*)b->d_sblocks[b->parity][s],
                          b->d_tiles[s], b->ntiles[s], info, b->h->phys, b->grid, st);
@@ -371,8 +390,17 @@ cudaError_t record_cycle(mhdvlct_batch* b, int dt_mode, cudaStream_t st) {
 extern "C" int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
                                     const double* widths, int nblocks, int ghost,
                                     int dtype, mhdvlct_batch** out) {
+  return mhdvlct_batch_create_ex(h, dims, widths, nblocks, ghost, dtype, 0, 0, out);
+}
+
+extern "C" int mhdvlct_batch_create_ex(mhdvlct_handle* h, const int* dims,
+                                       const double* widths, int nblocks, int ghost,
+                                       int dtype, int npassive, int gravity,
+                                       mhdvlct_batch** out) {
   if (!h || !dims || !widths || !out || nblocks <= 0) return MHD_ERR_INVALID;
   *out = nullptr;
+  if (npassive < 0 || npassive > 4 || (gravity != 0 && gravity != 1))
+    return fail(h, MHD_ERR_INVALID, "npassive must be 0..4 and gravity 0 or 1");
   if (dtype != MHD_DTYPE_F64 && dtype != MHD_DTYPE_F32)
     return fail(h, MHD_ERR_INVALID, "unknown dtype");
   if (h->euler) return fail(h, MHD_ERR_INVALID, "the batched form runs the vl scheme");
@@ -383,6 +411,8 @@ extern "C" int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
   b->dtype = dtype;
   b->nblocks = nblocks;
   b->g = ghost;
+  b->npass = npassive;
+  b->gravity = gravity;
   b->dims.assign(dims, dims + 3 * nblocks);
   b->widths.assign(widths, widths + 3 * nblocks);
   const size_t esz = dtype == MHD_DTYPE_F64 ? 8 : 4;
@@ -414,6 +444,14 @@ extern "C" int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
         if (pass == 0) O.ext[k] = used ? take(M) : (size_t)-1;
         else O.tmp[k] = used ? take(M) : (size_t)-1;
       }
+      // passive scalars and the acceleration follow the block's cell fields
+      // in the state region (a block's state stays one contiguous range)
+      for (int k = 0; k < 4; k++) {
+        if (pass == 0) O.pas[k] = k < npassive ? take(M) : (size_t)-1;
+        else O.ptmp[k] = k < npassive ? take(M) : (size_t)-1;
+      }
+      for (int d = 0; d < 3; d++)
+        if (pass == 0) O.acc[d] = gravity ? take(M) : (size_t)-1;
       for (int d = 0; d < 3; d++)
         if (pass == 1) O.tf[d] = h->mhd ? take(F[d]) : (size_t)-1;
       if (pass == 1) O.pres = take(M);
@@ -652,6 +690,9 @@ void fill_view(const mhdvlct_batch* b, int i, int parity, MhdBlockView* v) {
     v->bfieldi[d] = p(parity == 0 ? O.fa[d] : O.fb[d]);
   }
   v->pressure = p(O.pres);
+  for (int d = 0; d < 3; d++) v->acceleration[d] = p(O.acc[d]);
+  for (int k = 0; k < b->npass; k++) v->passive[k] = p(O.pas[k]);
+  v->npassive = b->npass;
 }
 }  // namespace
 

@@ -634,6 +634,7 @@ int aux_setup(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
   a.f = fieldset_of<R>(b);
   a.pressure = (R*)b->pressure;
   for (int k = 0; k < b->npassive; k++) a.pass[k] = (R*)b->passive[k];
+  for (int d = 0; d < 3; d++) a.accel[d] = (R*)b->acceleration[d];
   cudaError_t e = cudaMemcpyAsync(S.d_aux, &a, sizeof(a), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "aux upload");
   return MHD_OK;

@@ -15,6 +15,7 @@ template <class R> struct AuxBlock {
   FieldSet<R> f;     // fields (cell + face)
   R* pressure;       // optional [w] pressure field
   R* pass[4] = {nullptr, nullptr, nullptr, nullptr};  // passive scalars
+  R* accel[3] = {nullptr, nullptr, nullptr};          // acceleration_x/y/z
 };
 
 // ---------------------------------------------------------------------------
@@ -184,13 +185,14 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
   const int n[3] = {B.m[0] - 2 * g, B.m[1] - 2 * g, B.m[2] - 2 * g};
   for (int fs = 0; fs < nfield_slots; fs++) {
     // slots 0..8 cell fields, 9..11 face fields, 12 the pressure field,
-    // 13..16 passive scalars (Cello refreshes every field,
+    // 13..16 passive scalars, 17..19 the acceleration (Cello refreshes every field,
     // EnzoMethodMHDVlct.cpp:146-151)
     auto slot_ptr = [&](const AuxBlock<R>& X) -> R* {
       if (fs < NCELL) return X.f.c[fs];
       if (fs < NCELL + 3) return X.f.f[fs - NCELL];
       if (fs == NCELL + 3) return X.pressure;
-      return X.pass[fs - NCELL - 4];
+      if (fs < NCELL + 8) return X.pass[fs - NCELL - 4];
+      return X.accel[fs - NCELL - 8];
     };
     R* dst = slot_ptr(B);
     if (!dst) continue;
@@ -281,7 +283,8 @@ refresh_fast_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restric
       if (fs < NCELL) return X.f.c[fs];
       if (fs < NCELL + 3) return X.f.f[fs - NCELL];
       if (fs == NCELL + 3) return X.pressure;
-      return X.pass[fs - NCELL - 4];
+      if (fs < NCELL + 8) return X.pass[fs - NCELL - 4];
+      return X.accel[fs - NCELL - 8];
     };
     const int face = (fs >= NCELL && fs < NCELL + 3) ? fs - NCELL : -1;
     int e[3], lo[3], hi[3];

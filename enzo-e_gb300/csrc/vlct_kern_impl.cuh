@@ -137,9 +137,9 @@ cudaError_t launch_refresh<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, const int* n
   // field) x (largest divisor) < 2^32; bound the shell by the whole field
   const unsigned long long mm = (unsigned long long)max_m + 1;
   if (mm * mm * mm * mm < (1ull << 32))
-    refresh_fast_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 8, cpb);
+    refresh_fast_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 11, cpb);
   else
-    refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 8, cpb);
+    refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 11, cpb);
   return cudaGetLastError();
 }
 

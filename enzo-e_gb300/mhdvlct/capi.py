@@ -32,7 +32,7 @@ EXPORTED = (
     "mhdvlct_block_bfield_from_potential",
     "mhdvlct_block_timestep", "mhdvlct_fill_ghosts_periodic",
     "mhdvlct_refresh_faces", "mhdvlct_refresh_face_box", "mhdvlct_flux_correct",
-    "mhdvlct_batch_create", "mhdvlct_batch_destroy",
+    "mhdvlct_batch_create", "mhdvlct_batch_create_ex", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
     "mhdvlct_batch_refresh", "mhdvlct_batch_set_refresh_faces",
     "mhdvlct_batch_set_flux_correction", "mhdvlct_batch_step", "mhdvlct_batch_timestep",
@@ -151,6 +151,7 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_flux_correct.argtypes = [vp, P(MhdBlockView), ip, P(MhdFluxCorrection),
                                        P(MhdRefreshFace), ip, ctypes.c_uint, vp]
     L.mhdvlct_batch_create.argtypes = [vp, P(ip), P(dp), ip, ip, ip, P(vp)]
+    L.mhdvlct_batch_create_ex.argtypes = [vp, P(ip), P(dp), ip, ip, ip, ip, ip, P(vp)]
     L.mhdvlct_batch_destroy.argtypes = [vp]
     L.mhdvlct_batch_block_view.argtypes = [vp, ip, P(MhdBlockView)]
     L.mhdvlct_batch_set_neighbors.argtypes = [vp, P(ip)]

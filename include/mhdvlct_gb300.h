@@ -293,6 +293,17 @@ typedef struct mhdvlct_batch mhdvlct_batch;
 int mhdvlct_batch_create(mhdvlct_handle* h, const int* dims,
                          const double* widths, int nblocks, int ghost,
                          int dtype, mhdvlct_batch** out);
+/* As mhdvlct_batch_create, with npassive (0..4) passive scalars in
+ * conserved form and, with gravity = 1, acceleration_x/y/z fields in every
+ * block (MhdBlockView::passive / acceleration of mhdvlct_batch_block_view):
+ * the scalars are advected and the gravity source is added on the full-dt
+ * stage exactly as mhdvlct_block_step does, and the refresh covers both, as
+ * Cello refreshes every field (EnzoMethodMHDVlct.cpp:146-151).  The
+ * acceleration is the caller's: no step writes it. */
+int mhdvlct_batch_create_ex(mhdvlct_handle* h, const int* dims,
+                            const double* widths, int nblocks, int ghost,
+                            int dtype, int npassive, int gravity,
+                            mhdvlct_batch** out);
 int mhdvlct_batch_destroy(mhdvlct_batch* b);
 /* Device pointers of block i's current state (valid until the next step). */
 int mhdvlct_batch_block_view(mhdvlct_batch* b, int i, MhdBlockView* out);

@@ -1232,7 +1232,7 @@ void fill_fields(OracleBlock* blocks, int nbx, int nby, int nbz) {
   const int g = blocks[0].g;
   const int n[3] = {blocks[0].nx, blocks[0].ny, blocks[0].nz};
   const int m[3] = {n[0] + 2 * g, n[1] + 2 * g, n[2] + 2 * g};
-  const int nfield = 13;
+  const int nfield = 20;  // every field (EnzoMethodMHDVlct.cpp:146-151)
   // copy sources first so that the refresh reads pre-refresh values only
   for (int f = 0; f < nfield; f++) {
     int face = -1;
@@ -1243,7 +1243,9 @@ void fill_fields(OracleBlock* blocks, int nbx, int nby, int nbz) {
         case 3: return b.vz; case 4: return b.etot; case 5: return b.eint;
         case 6: return b.bx; case 7: return b.by; case 8: return b.bz;
         case 9: return b.bfx; case 10: return b.bfy; case 11: return b.bfz;
-        default: return b.pressure;
+        case 12: return b.pressure;
+        case 13: return b.ax; case 14: return b.ay; case 15: return b.az;
+        default: return f - 16 < b.npassive ? b.passive[f - 16] : nullptr;
       }
     };
     if (f == 9) face = 0;

@@ -23,13 +23,14 @@ KEYS = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
 
 
 class Batch:
-    def __init__(self, meth, dims, widths, dtype=capi.MHD_DTYPE_F64, ghost=3):
+    def __init__(self, meth, dims, widths, dtype=capi.MHD_DTYPE_F64, ghost=3,
+                 npassive=0, gravity=False):
         n = len(dims)
         d = (ctypes.c_int * (3 * n))(*[int(v) for t in dims for v in t])
         w = (ctypes.c_double * (3 * n))(*[float(v) for t in widths for v in t])
         h = ctypes.c_void_p()
-        rc = capi.lib().mhdvlct_batch_create(meth.handle, d, w, n, ghost, dtype,
-                                             ctypes.byref(h))
+        rc = capi.lib().mhdvlct_batch_create_ex(meth.handle, d, w, n, ghost, dtype,
+                                                npassive, int(gravity), ctypes.byref(h))
         capi.check(rc, meth.handle, "batch_create")
         self.h, self.meth, self.n = h, meth, n
         self.dims, self.dtype = dims, dtype
@@ -51,7 +52,11 @@ class Batch:
                 "total_energy": v.total_energy, "bfield_x": v.bfield[0],
                 "bfield_y": v.bfield[1], "bfield_z": v.bfield[2],
                 "bfieldi_x": v.bfieldi[0], "bfieldi_y": v.bfieldi[1],
-                "bfieldi_z": v.bfieldi[2], "pressure": v.pressure}
+                "bfieldi_z": v.bfieldi[2], "pressure": v.pressure,
+                "acceleration_x": v.acceleration[0], "acceleration_y": v.acceleration[1],
+                "acceleration_z": v.acceleration[2]}
+        for k in range(v.npassive):
+            ptrs[f"passive_{k}"] = v.passive[k]
         shapes = {"bfieldi_x": (mz, my, mx + 1), "bfieldi_y": (mz, my + 1, mx),
                   "bfieldi_z": (mz + 1, my, mx)}
         for k, p in ptrs.items():
@@ -374,3 +379,71 @@ def _memset(ptr, nbytes):
     if _cudart is None:
         _cudart = _load_cudart()
     assert _cudart.cudaMemset(ptr, 0x7F, nbytes) == 0
+
+
+def test_graph_run_gravity_passive_matches_oracle_cycles():
+    """Blocks with acceleration fields and two passive scalars: graph-captured
+    cycles (timestep, global min dt, refresh of every field, both stages
+    with the gravity source on the full-dt one) equal the oracle's cycle
+    bit for bit in FP64, the scalars and the refreshed acceleration
+    included."""
+    meth = B.EnzoMethodMHDVlct()
+    nb, N, g, n = 2, 16, 3, 8
+    blocks, w = ic.turbulent_box(N=N, nb=nb, g=g, seed=5, mach=1.0)
+    rng = np.random.default_rng(17)
+    m = n + 2 * g
+    act = (slice(g, g + n),) * 3
+    for s in blocks:
+        for k in ("acceleration_x", "acceleration_y", "acceleration_z"):
+            s[k] = np.zeros((m, m, m))  # ghosts come from the refresh
+            s[k][act] = 0.3 * (rng.random((n, n, n)) - 0.5)
+        for k in range(2):
+            s[f"passive_{k}"] = s["density"] * (0.2 + 0.6 * rng.random((m, m, m)))
+    bt = Batch(meth, [(n,) * 3] * 8, [w] * 8, npassive=2, gravity=True)
+    nbr = ic.brick_neighbors(nb)
+    capi.check(capi.lib().mhdvlct_batch_set_neighbors(
+        bt.h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())))
+    for i, s in enumerate(blocks):
+        bt.upload(i, s)
+    oname = dict(ic.ORACLE_NAME, acceleration_x="ax", acceleration_y="ay",
+                 acceleration_z="az", passive_0="pass0", passive_1="pass1")
+    obs = []
+    for s in blocks:
+        ob = O.Block(n, g, w, mhd=True, gravity=True, npassive=2)
+        for k, v in s.items():
+            if oname[k] in ob.f:
+                ob.f[oname[k]][...] = v
+        obs.append(ob)
+    ncyc = 3
+    t = ctypes.c_double()
+    capi.check(capi.lib().mhdvlct_batch_run(bt.h, ncyc, 0, ctypes.byref(t), None))
+    prm = oracle_params(courant=meth.courant)
+    tt = 0.0
+    for _ in range(ncyc):
+        dt = min(O.timestep(prm, ob) for ob in obs)
+        O.fill_ghosts_brick(obs, nb, nb, nb)
+        for ob in obs:
+            O.step(prm, ob, dt)
+        tt += dt
+    assert t.value == tt
+    for i in range(8):
+        got = bt.download(i)
+        assert set(got) >= {"passive_0", "passive_1", "acceleration_z"}
+        for k in KEYS[:8] + ("passive_0", "passive_1"):
+            assert np.array_equal(got[k][act], obs[i].f[oname[k]][act]), (i, k)
+        for k in ("acceleration_x", "acceleration_y", "acceleration_z"):
+            assert np.array_equal(got[k], obs[i].f[oname[k]]), (i, k)
+        # the source and the scalars took effect
+        assert not np.array_equal(got["passive_0"][act], blocks[i]["passive_0"][act])
+
+
+def test_batch_create_ex_rejects_bad_options():
+    meth = B.EnzoMethodMHDVlct()
+    d = (ctypes.c_int * 3)(8, 8, 8)
+    w = (ctypes.c_double * 3)(0.1, 0.1, 0.1)
+    h = ctypes.c_void_p()
+    for npass, grav in ((5, 0), (-1, 0), (0, 2)):
+        rc = capi.lib().mhdvlct_batch_create_ex(meth.handle, d, w, 1, 3,
+                                                capi.MHD_DTYPE_F64, npass, grav,
+                                                ctypes.byref(h))
+        assert rc == capi.MHD_ERR_INVALID and not h.value
