@@ -61,7 +61,7 @@ def _args():
     ap.add_argument("--cpu-sample-blocks", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mode", default="main",
-                    choices=["main", "amr", "serve", "precision", "fc", "smr"],
+                    choices=["main", "amr", "serve", "precision", "fc", "smr", "extras"],
                     help="main: the contract line; amr / serve / precision: the "
                          "mixed-size block set, the serving stream, the FP32-vs-FP64 "
                          "study (one JSON line each)")
@@ -310,9 +310,11 @@ def view_pointers(v):
             "bfieldi_z": v.bfieldi[2]}
 
 
-def make_batch_general(meth, blocks, dims, widths, dtype, nbr, ghost=GHOST):
+def make_batch_general(meth, blocks, dims, widths, dtype, nbr, ghost=GHOST, npass=0,
+                       gravity=False):
     """Batch of arbitrary blocks: dims/widths per block, nbr the 27-neighbour
-    table (nblocks x 27); blocks' host arrays are copied into the pool."""
+    table (nblocks x 27); blocks' host arrays are copied into the pool (with
+    npass passive scalars passive_k and, with gravity, acceleration_x/y/z)."""
     import numpy as np
     from mhdvlct import capi
     n_blk = len(dims)
@@ -320,8 +322,9 @@ def make_batch_general(meth, blocks, dims, widths, dtype, nbr, ghost=GHOST):
     ws = (ctypes.c_double * (3 * n_blk))(*[float(x) for w in widths for x in w])
     h = ctypes.c_void_p()
     L = capi.lib()
-    capi.check(L.mhdvlct_batch_create(meth.handle, cd, ws, n_blk, ghost, dtype,
-                                      ctypes.byref(h)), meth.handle, "batch_create")
+    capi.check(L.mhdvlct_batch_create_ex(meth.handle, cd, ws, n_blk, ghost, dtype, npass,
+                                         int(gravity), ctypes.byref(h)),
+               meth.handle, "batch_create")
     nbr = np.ascontiguousarray(nbr, dtype=np.int32)
     capi.check(L.mhdvlct_batch_set_neighbors(
         h, nbr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), meth.handle, "nbr")
@@ -330,7 +333,12 @@ def make_batch_general(meth, blocks, dims, widths, dtype, nbr, ghost=GHOST):
     for i, blk in enumerate(blocks):
         v = capi.MhdBlockView()
         capi.check(L.mhdvlct_batch_block_view(h, i, ctypes.byref(v)))
-        for k, p in view_pointers(v).items():
+        ptrs = view_pointers(v)
+        for d, ax in enumerate("xyz"):
+            ptrs[f"acceleration_{ax}"] = v.acceleration[d]
+        for k in range(v.npassive):
+            ptrs[f"passive_{k}"] = v.passive[k]
+        for k, p in ptrs.items():
             if not p or k not in blk:
                 continue
             a = np.ascontiguousarray(blk[k], dtype=npdt)
@@ -652,6 +660,52 @@ def run_smr(a, root=8, n=32, fc=False):
             "finite": all(np.isfinite(list(diag)))}
 
 
+def run_extras(a, npass=2):
+    """The gravity source and passive scalars in the batched cycle: the
+    turbulent box (HLLD + PLM, FP32, default tiles) advanced by graph-captured
+    cycles (timestep, global min dt, refresh, both stages), without and with
+    acceleration fields and npass passive scalars.  Wall clock around
+    a.steps cycles of one mhdvlct_batch_run call, synchronised on both
+    sides."""
+    import numpy as np
+    import torch
+    from mhdvlct import block as B, capi, ic
+    meth = B.EnzoMethodMHDVlct(riemann_solver="hlld", reconstruct_method="plm",
+                               courant=COURANT)
+    blocks, w = ic.turbulent_box(N=a.n, nb=a.nb, g=GHOST, seed=1, mach=2.0)
+    n = a.n // a.nb
+    m = n + 2 * GHOST
+    rng = np.random.default_rng(2)
+    for st in blocks:
+        for ax in "xyz":
+            st[f"acceleration_{ax}"] = 0.1 * (rng.random((m, m, m)) - 0.5)
+        for k in range(npass):
+            st[f"passive_{k}"] = st["density"] * (0.2 + 0.6 * rng.random((m, m, m)))
+    nblk = len(blocks)
+    L = capi.lib()
+    steps = max(1, a.steps)
+    out = {"mode": "extras", "workload": f"turbulent box {a.n}^3 in {nblk} blocks of {n}^3 "
+                                         f"(+{GHOST} ghosts), HLLD+PLM, FP32",
+           "unit": "zone-updates/s", "steps": steps}
+    for tag, (np_, grav) in (("plain", (0, False)), ("gravity", (0, True)),
+                             ("passive", (npass, False)), ("gravity_passive", (npass, True))):
+        h = make_batch_general(meth, blocks, [(n, n, n)] * nblk, [tuple(w)] * nblk,
+                               capi.MHD_DTYPE_F32, ic.brick_neighbors(a.nb), npass=np_,
+                               gravity=grav)
+        t = ctypes.c_double()
+        capi.check(L.mhdvlct_batch_run(h, max(3, a.warmup), 0, ctypes.byref(t), None))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        capi.check(L.mhdvlct_batch_run(h, steps, 0, ctypes.byref(t), None))
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        L.mhdvlct_batch_destroy(h)
+        out[tag] = a.n ** 3 * steps / el
+    out["npassive"] = npass
+    out["overhead_gravity_passive"] = out["plain"] / out["gravity_passive"] - 1.0
+    return out
+
+
 def run_fc(a, nblocks=64, n=32):
     """Flux correction on the plain per-block path: HLLC + PLM hydro blocks
     (dual energy on), each advanced by timestep + compute, with and without
@@ -842,6 +896,8 @@ def main():
                 out = run_fc(a)
             elif a.mode == "smr":
                 out = run_smr(a, root=a.smr_root, fc=a.smr_fc)
+            elif a.mode == "extras":
+                out = run_extras(a)
             else:
                 out = run_precision(a, cycles=a.precision_cycles, N=a.precision_n)
             print(json.dumps(out), flush=True)

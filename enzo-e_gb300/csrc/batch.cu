@@ -140,7 +140,7 @@ TileChoice choice_for(const mhdvlct_batch* b, int i) {
   const StagePlan sp = stage_plan(b->h);
   for (int s = 0; s < 2; s++)
     if (c.tile_x[s] <= 0 || c.tile_y[s] <= 0) {
-      const int t = default_tile(b->dtype, b->h->solver, sp.recon[s], b->h->de);
+      const int t = default_tile(b->dtype, b->h->solver, sp.recon[s], b->h->de, b->npass);
       c.tile_x[s] = c.tile_y[s] = t;
     }
   if (!tuned) {
@@ -1160,7 +1160,8 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
       std::vector<TileChoice> cands;
       for (auto& sh : shapes) {
         if (stage_smem<R>(b->h->solver, sp.recon[s], b->h->de != 0,
-                          std::max(sh.first, other_tx), std::max(sh.second, other_ty)) >
+                          std::max(sh.first, other_tx), std::max(sh.second, other_ty),
+                          b->npass) >
             smem_cap)
           continue;
         for (int zc : {0, 16}) {

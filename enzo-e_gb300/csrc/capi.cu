@@ -103,10 +103,10 @@ FieldSet<R> fieldset_of(const MhdBlockView* b) {
 template FieldSet<double> fieldset_of<double>(const MhdBlockView*);
 template FieldSet<float> fieldset_of<float>(const MhdBlockView*);
 
-int default_tile(int dtype, int solver, int recon, int de) {
-  // largest tile whose shared memory fits the CTAs an SM holds at once
-  // (227 KB per SM): one CTA for FP64, three for the FP32 NN stage, two for
-  // the other FP32 stages
+int default_tile(int dtype, int solver, int recon, int de, int np) {
+  // largest tile whose shared memory (np passive scalars included) fits the
+  // CTAs an SM holds at once (227 KB per SM): one CTA for FP64, three for
+  // the FP32 NN stage, two for the other FP32 stages
   const int cap = (dtype == MHD_DTYPE_F64) ? 200 * 1024
                   : (recon == RECON_NN)    ? 72 * 1024
                                            : 110 * 1024;
@@ -115,8 +115,8 @@ int default_tile(int dtype, int solver, int recon, int de) {
                                                  : TileLimits<float>::TMAX);
        t++) {
     const size_t b = (dtype == MHD_DTYPE_F64)
-                         ? stage_smem<double>(solver, recon, de != 0, t, t)
-                         : stage_smem<float>(solver, recon, de != 0, t, t);
+                         ? stage_smem<double>(solver, recon, de != 0, t, t, np)
+                         : stage_smem<float>(solver, recon, de != 0, t, t, np);
     if (b <= (size_t)cap) best = t;
   }
   return best;

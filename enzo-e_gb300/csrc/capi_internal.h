@@ -60,7 +60,7 @@ template <class R>
 vlct::FieldSet<R> fieldset_of(const MhdBlockView* b);
 
 // Default tile extent for a precision (fits the shared-memory budget).
-int default_tile(int dtype, int solver, int recon, int de);
+int default_tile(int dtype, int solver, int recon, int de, int np = 0);
 
 // Mesh ghost refresh (refresh.cu): a validated plan of refresh faces over a
 // set of block views -- the per-block field pointer table and the device

@@ -69,11 +69,11 @@ cudaError_t stage_de(int recon, bool de, const StageBlock<R>* b,
 }
 
 template <class R, int SOLVER, bool DE>
-size_t smem_recon(int recon, int tx, int ty) {
+size_t smem_recon(int recon, int tx, int ty, int np) {
   switch (recon) {
-    case RECON_NN: return stage_smem_bytes<R, SOLVER, RECON_NN, DE>(tx, ty);
-    case RECON_PLM: return stage_smem_bytes<R, SOLVER, RECON_PLM, DE>(tx, ty);
-    default: return stage_smem_bytes<R, SOLVER, RECON_PLM_ATHENA, DE>(tx, ty);
+    case RECON_NN: return stage_smem_bytes<R, SOLVER, RECON_NN, DE>(tx, ty, np);
+    case RECON_PLM: return stage_smem_bytes<R, SOLVER, RECON_PLM, DE>(tx, ty, np);
+    default: return stage_smem_bytes<R, SOLVER, RECON_PLM_ATHENA, DE>(tx, ty, np);
   }
 }
 }  // namespace
@@ -94,14 +94,14 @@ cudaError_t launch_stage<VLCT_REAL>(int solver, int recon, bool de,
 }
 
 template <>
-size_t stage_smem<VLCT_REAL>(int solver, int recon, bool de, int tx, int ty) {
+size_t stage_smem<VLCT_REAL>(int solver, int recon, bool de, int tx, int ty, int np) {
   // the solver changes only NF (hydro vs MHD)
   if (solver == SOLVER_HLLC) {
-    return de ? smem_recon<VLCT_REAL, SOLVER_HLLC, true>(recon, tx, ty)
-              : smem_recon<VLCT_REAL, SOLVER_HLLC, false>(recon, tx, ty);
+    return de ? smem_recon<VLCT_REAL, SOLVER_HLLC, true>(recon, tx, ty, np)
+              : smem_recon<VLCT_REAL, SOLVER_HLLC, false>(recon, tx, ty, np);
   }
-  return de ? smem_recon<VLCT_REAL, SOLVER_HLLD, true>(recon, tx, ty)
-            : smem_recon<VLCT_REAL, SOLVER_HLLD, false>(recon, tx, ty);
+  return de ? smem_recon<VLCT_REAL, SOLVER_HLLD, true>(recon, tx, ty, np)
+            : smem_recon<VLCT_REAL, SOLVER_HLLD, false>(recon, tx, ty, np);
 }
 
 template <>
