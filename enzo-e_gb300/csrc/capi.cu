@@ -850,8 +850,10 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     off += align_up(bytes);
     return o;
   };
-  size_t o_tmp[NCELL], o_tf[3], o_ff[3];
+  size_t o_tmp[NCELL], o_tf[3], o_ff[3], o_tp[4];
+  const int np = b->npassive;
   for (int k = 0; k < NCELL; k++) o_tmp[k] = take(M * sizeof(R));
+  for (int k = 0; k < np; k++) o_tp[k] = take(M * sizeof(R));  // half-step scalars
   for (int d = 0; d < 3; d++) o_tf[d] = take(F[d] * sizeof(R));
   for (int d = 0; d < 3; d++) o_ff[d] = take(F[d] * sizeof(R));
   const size_t o_dt = take(sizeof(double));
@@ -869,6 +871,7 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   if (rc) return rc;
   PlainScratch<R> S;
   for (int k = 0; k < NCELL; k++) S.tmp[k] = (R*)(base + o_tmp[k]);
+  for (int k = 0; k < 4; k++) S.tpass[k] = k < np ? (R*)(base + o_tp[k]) : nullptr;
   for (int d = 0; d < 3; d++) {
     S.tface[d] = (R*)(base + o_tf[d]);
     S.fface[d] = (R*)(base + o_ff[d]);
@@ -894,6 +897,14 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     B.dt = S.d_dt;
     B.base = ext;
     for (int d = 0; d < 3; d++) B.accel[d] = (const R*)b->acceleration[d];
+    for (int k = 0; k < np; k++) {
+      // as mhdvlct_block_step: vl writes the half step into scratch and then
+      // the caller's scalars; euler reads a copy (made below)
+      R* ep = (R*)b->passive[k];
+      B.pass_base[k] = ep;
+      B.pass_cur[k] = (sp.nstages == 1 || i == 1) ? S.tpass[k] : ep;
+      B.pass_out[k] = (sp.nstages == 2 && i == 0) ? S.tpass[k] : ep;
+    }
     if (sp.nstages == 1) {
       B.cur = tmp;
       for (int d = 0; d < 3; d++) B.cur.f[d] = ext.f[d];
@@ -926,6 +937,11 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
       e = cudaMemcpyAsync(S.tmp[k], ext.c[k], M * sizeof(R), cudaMemcpyDeviceToDevice, st);
       if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
     }
+    for (int k = 0; k < np; k++) {
+      e = cudaMemcpyAsync(S.tpass[k], b->passive[k], M * sizeof(R), cudaMemcpyDeviceToDevice,
+                          st);
+      if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
+    }
   }
   const StageTile* dtiles[2] = {S.d_tiles, S.d_tiles + ntiles[0]};
   for (int i = 0; i < sp.nstages; i++) {
@@ -941,6 +957,7 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     // EnzoMHDIntegratorStageCommands.cpp:279: the gravity source enters the
     // stage with index 1 (the full-dt stage of vl; never with euler)
     info.gravity = (i == 1 && b->acceleration[0] != nullptr) ? 1 : 0;
+    info.npass = np;
     e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, dtiles[i],
                         ntiles[i], info, h->phys, 0, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");
@@ -961,10 +978,6 @@ extern "C" int mhdvlct_block_step_noalloc(mhdvlct_handle* h, const MhdBlockView*
   if (!h) return MHD_ERR_INVALID;
   int rc = check_view(h, b);
   if (rc) return rc;
-  if (b->npassive > 0)
-    return fail(h, MHD_ERR_INVALID,
-                "mhdvlct_block_step_noalloc does not advect passive scalars "
-                "(use mhdvlct_block_step)");
   if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
   cudaStream_t st = (cudaStream_t)stream;
   return b->dtype == MHD_DTYPE_F64 ? block_step_noalloc_t<double>(h, b, dt, st)

@@ -286,6 +286,9 @@ refresh_fast_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restric
       if (fs < NCELL + 8) return X.pass[fs - NCELL - 4];
       return X.accel[fs - NCELL - 8];
     };
+    // a field this block does not hold: skip it before the barriers (the
+    // test is uniform over the CTA)
+    if (!slot_ptr(B)) continue;
     const int face = (fs >= NCELL && fs < NCELL + 3) ? fs - NCELL : -1;
     int e[3], lo[3], hi[3];
     for (int a = 0; a < 3; a++) {

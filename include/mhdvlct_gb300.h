@@ -159,8 +159,9 @@ int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
  * is one file-scope __device__ array of 8 MiB (8388608 bytes) per device,
  * whose address is taken with cudaGetSymbolAddress on the first call on each
  * device and cached.  Make that first call on a device outside stream
- * capture.  A block whose scratch (all cell fields and two sets of face
- * fields at the ghosted extents, plus descriptors) exceeds 8 MiB, or whose
+ * capture.  A block whose scratch (all cell fields, the passive scalars'
+ * half step and two sets of face fields at the ghosted extents, plus
+ * descriptors) exceeds 8 MiB, or whose
  * stage needs more than 512 tiles, is rejected with MHD_ERR_INVALID and a
  * message naming the bytes needed (an FP64 block of 32^3 cells with 3 ghost
  * zones needs about 6.7 MB).  Nothing in the array has to start at zero:

@@ -84,8 +84,15 @@ def test_periodic_refresh_covers_passive():
         assert np.array_equal(got[k], np.pad(inner, g, mode="wrap")), k
 
 
-def test_noalloc_refuses_passive():
-    meth, blk, _, _ = _pair("hllc", "plm", False, "vl", torch.float64, npass=1)
+def test_noalloc_passive_step_bit_exact():
+    # the no-alloc entry keeps the scalars' half step in its static array
+    meth, blk, ob, prm = _pair("hllc", "plm", False, "vl", torch.float64, npass=2)
+    dt = O.timestep(prm, ob)
+    assert meth.timestep(blk) == dt
+    O.step(prm, ob, dt)
     v = blk.view()
-    rc = capi.lib().mhdvlct_block_step_noalloc(meth.handle, ctypes.byref(v), 1e-3, None)
-    assert rc == capi.MHD_ERR_INVALID
+    rc = capi.lib().mhdvlct_block_step_noalloc(meth.handle, ctypes.byref(v), dt, None)
+    assert rc == capi.MHD_OK
+    torch.cuda.synchronize()
+    for k, a in blk.to_numpy().items():
+        assert np.array_equal(a, ob.f[_oname(k)]), k

@@ -67,6 +67,34 @@ def test_noalloc_matches_allocating_step_two_calls(solver, recon, de, scheme, n,
         _same(a, b)
 
 
+@pytest.mark.parametrize("solver,recon,de,scheme", [
+    ("hlld", "plm", False, "vl"), ("hllc", "plm", True, "euler")])
+def test_noalloc_passive_scalars_match_allocating_step(solver, recon, de, scheme):
+    # three passive scalars: their half step lives in the static array too
+    n, npass = (8, 7, 6), 3
+    mhd = solver != "hllc"
+    state, w = ic.smooth_block(n, 3, seed=23, mhd=mhd, dual_energy=de)
+    rng = np.random.default_rng(5)
+    for k in range(npass):
+        state[f"passive_{k}"] = state["density"] * (0.2 + 0.6 * rng.random(state["density"].shape))
+    meth = B.EnzoMethodMHDVlct(
+        mhd_choice="constrained_transport" if mhd else "no_bfield",
+        riemann_solver=solver, reconstruct_method=recon, time_scheme=scheme,
+        dual_energy=de)
+    a, b = (B.Block(n, 3, w, mhd=mhd, dual_energy=de, dtype=torch.float64, npassive=npass)
+            for _ in range(2))
+    a.load_numpy(state)
+    b.load_numpy(state)
+    for _ in range(2):
+        dt = meth.timestep(a)
+        assert meth.timestep(b) == dt
+        meth.compute(a, dt)
+        assert _noalloc_step(meth, b, dt) == capi.MHD_OK
+        torch.cuda.synchronize()
+        _same(a, b)
+    assert "passive_2" in a.to_numpy()
+
+
 def test_noalloc_geometry_change_between_calls():
     # a larger block after a smaller one reuses the same static array
     for n in ((6, 6, 6), (16, 10, 12), (6, 6, 6)):
