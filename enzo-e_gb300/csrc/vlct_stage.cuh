@@ -313,6 +313,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         const int x = hx0 + i, y = hy0 + j;
         // face index f along d: the face between cells f and f+1
         int off[4];  // s_prim offsets of the cells f-1 .. f+2 along d
+        int sl[4];   // their ring slots (for the passive planes' offsets)
         const R* bface;
         R* dst;
         const int r = j * HP + i;
@@ -321,7 +322,10 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           if (!inr(fz, S, m2 - 1 - S) || !inr(x, S, m0 - S) || !inr(y, S, m1 - S))
             continue;
 #pragma unroll
-          for (int k = 0; k < 4; k++) off[k] = poff((fz - 1 + k + NRING) % NRING, x, y);
+          for (int k = 0; k < 4; k++) {
+            sl[k] = (fz - 1 + k + NRING) % NRING;
+            off[k] = poff(sl[k], x, y);
+          }
           bface = B.cur.f[2] + ((size_t)(fz + 1) * cstr_z + (size_t)y * cstr_y + x);
           dst = s_zf + (size_t)(fz & 1) * NF * G + r;
         } else {
@@ -330,14 +334,20 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           if (d == 0) {
             if (!inr(x, S, m0 - 1 - S) || !inr(y, S, m1 - S)) continue;
 #pragma unroll
-            for (int k = 0; k < 4; k++) off[k] = poff(slot, x - 1 + k, y);
+            for (int k = 0; k < 4; k++) {
+              sl[k] = slot;
+              off[k] = poff(slot, x - 1 + k, y);
+            }
             bface = B.cur.f[0] + ((size_t)pl * ((size_t)m1 * (m0 + 1)) +
                                   (size_t)y * (m0 + 1) + (x + 1));
             dst = s_xf + (size_t)(pl & 1) * NF * G + r;
           } else {
             if (!inr(y, S, m1 - 1 - S) || !inr(x, S, m0 - S)) continue;
 #pragma unroll
-            for (int k = 0; k < 4; k++) off[k] = poff(slot, x, y - 1 + k);
+            for (int k = 0; k < 4; k++) {
+              sl[k] = slot;
+              off[k] = poff(slot, x, y - 1 + k);
+            }
             bface = B.cur.f[1] + ((size_t)pl * ((size_t)(m1 + 1) * m0) +
                                   (size_t)(y + 1) * m0 + x);
             dst = s_yf + (size_t)(pl & 1) * NF * G + r;
@@ -408,14 +418,16 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         // times the density flux; stored beside the face's other fluxes
         for (int k = 0; k < NP; k++) {
           const R* w = sm + Ls.o_pprim + k * PQ;
-          const int st = NP * PQ;  // ring-slot stride of the passive planes
-          auto at = [&](int o) { return w[(o / (NQ * PQ)) * st + (o % (NQ * PQ))]; };
+          // cell j of the stencil: ring slot sl[j] holds NP passive planes
+          // instead of NQ primitive planes, at the same in-plane position
+          const int dq = (NP - NQ) * PQ;
+          auto at = [&](int j) { return w[off[j] + sl[j] * dq]; };
           R lv, rv;
           if (RECON == RECON_NN) {
-            lv = at(off[1]);
-            rv = at(off[2]);
+            lv = at(1);
+            rv = at(2);
           } else {
-            const R a = at(off[0]), b0 = at(off[1]), b1 = at(off[2]), c = at(off[3]);
+            const R a = at(0), b0 = at(1), b1 = at(2), c = at(3);
             R dl, dr;
             if (RECON == RECON_PLM) {
               dl = limiter_enzo_rk(a, b0, b1, theta);
