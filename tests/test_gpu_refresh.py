@@ -256,3 +256,57 @@ def test_three_level_refresh_bit_exact(dtype):
         for s_, a in r.items():
             assert np.isfinite(a).all(), (i, SLOT_NAME[s_])
             assert np.array_equal(got[SLOT_NAME[s_]], a), (i, SLOT_NAME[s_])
+
+
+def test_smr_batch_graph_gravity_passive_bit_exact():
+    """The batched SMR cycle with the acceleration and one passive scalar in
+    every leaf: the mesh refresh carries both across levels (slots 10..13)
+    and the stages advect the scalar and add the gravity source, bit for bit
+    with the oracle in FP64."""
+    from test_gpu_batch import Batch
+    mesh, n, g, states, widths = _smr_case(False)
+    rng = np.random.default_rng(29)
+    act = tuple(slice(g, g + k) for k in n[::-1])
+    for st in states:
+        for ax in "xyz":
+            a = np.full_like(st["density"], np.nan)
+            a[act] = 0.2 * (rng.random(a[act].shape) - 0.5)
+            st[f"acceleration_{ax}"] = a
+        p = np.full_like(st["density"], np.nan)
+        p[act] = st["density"][act] * (0.2 + 0.6 * rng.random(p[act].shape))
+        st["passive_0"] = p
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    prm = oracle_params("hllc", "plm", courant=0.4)
+    L = capi.lib()
+    bt = Batch(meth, [n] * len(states), widths, ghost=g, npassive=1, gravity=True)
+    for i, st in enumerate(states):
+        bt.upload(i, st)
+    farr, nf = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    capi.check(L.mhdvlct_batch_set_refresh_faces(bt.h, farr, nf, cons), meth.handle, "faces")
+    capi.check(L.mhdvlct_batch_refresh(bt.h, None), meth.handle, "refresh")
+    capi.check(L.mhdvlct_batch_run(bt.h, 3, 0, None, None), meth.handle, "run")
+    oname = dict(ic.ORACLE_NAME, acceleration_x="ax", acceleration_y="ay",
+                 acceleration_z="az", passive_0="pass0")
+    oblocks, slots = [], []
+    for st, w in zip(states, widths):
+        ob = O.Block(n, g, w, mhd=False, gravity=True, npassive=1)
+        for k, v in st.items():
+            ob.f[oname[k]][...] = v
+        oblocks.append(ob)
+        names = {0: "rho", 1: "vx", 2: "vy", 3: "vz", 4: "etot", 9: "pressure",
+                 10: "ax", 11: "ay", 12: "az", 13: "pass0"}
+        slots.append({s: ob.f[k] for s, k in names.items()})
+    ofaces = mesh.face_ints()
+    O.refresh_faces(slots, n, (g,) * 3, ofaces, cons)
+    for _ in range(3):
+        dt = min(O.timestep(prm, ob) for ob in oblocks)
+        O.refresh_faces(slots, n, (g,) * 3, ofaces, cons)
+        for ob in oblocks:
+            O.step(prm, ob, dt)
+    for i, ob in enumerate(oblocks):
+        got = bt.download(i)
+        for k in ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
+                  "passive_0", "acceleration_x", "acceleration_y", "acceleration_z"):
+            assert np.array_equal(got[k], ob.f[oname[k]], equal_nan=True), (i, k)
