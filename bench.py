@@ -662,9 +662,10 @@ def run_smr(a, root=8, n=32, fc=False):
 
 def run_extras(a, npass=2):
     """The gravity source and passive scalars in the batched cycle: the
-    turbulent box (HLLD + PLM, FP32, default tiles) advanced by graph-captured
-    cycles (timestep, global min dt, refresh, both stages), without and with
-    acceleration fields and npass passive scalars.  Wall clock around
+    turbulent box (HLLD + PLM, FP32) advanced by graph-captured cycles
+    (timestep, global min dt, refresh, both stages), without and with
+    acceleration fields and npass passive scalars, each variant with default
+    tiles and (unless --no-tune) with the autotuner's.  Wall clock around
     a.steps cycles of one mhdvlct_batch_run call, synchronised on both
     sides."""
     import numpy as np
@@ -693,16 +694,24 @@ def run_extras(a, npass=2):
                                capi.MHD_DTYPE_F32, ic.brick_neighbors(a.nb), npass=np_,
                                gravity=grav)
         t = ctypes.c_double()
-        capi.check(L.mhdvlct_batch_run(h, max(3, a.warmup), 0, ctypes.byref(t), None))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        capi.check(L.mhdvlct_batch_run(h, steps, 0, ctypes.byref(t), None))
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
+        for tuned in ((False, True) if not a.no_tune else (False,)):
+            if tuned:
+                buf = ctypes.create_string_buffer(4096)
+                capi.check(L.mhdvlct_batch_autotune(h, 2, buf, 4096, None), meth.handle,
+                           "autotune")
+            capi.check(L.mhdvlct_batch_run(h, max(3, a.warmup), 0, ctypes.byref(t), None))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            capi.check(L.mhdvlct_batch_run(h, steps, 0, ctypes.byref(t), None))
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+            out[tag + ("_tuned" if tuned else "")] = a.n ** 3 * steps / el
         L.mhdvlct_batch_destroy(h)
-        out[tag] = a.n ** 3 * steps / el
     out["npassive"] = npass
     out["overhead_gravity_passive"] = out["plain"] / out["gravity_passive"] - 1.0
+    if not a.no_tune:
+        out["overhead_gravity_passive_tuned"] = (
+            out["plain_tuned"] / out["gravity_passive_tuned"] - 1.0)
     return out
 
 
