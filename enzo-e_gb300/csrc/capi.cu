@@ -107,9 +107,10 @@ int default_tile(int dtype, int solver, int recon, int de, int np) {
   // largest tile whose shared memory (np passive scalars included) fits the
   // CTAs an SM holds at once (227 KB per SM): one CTA for FP64, three for
   // the FP32 NN stage, two for the other FP32 stages
-  const int cap = (dtype == MHD_DTYPE_F64) ? 200 * 1024
-                  : (recon == RECON_NN)    ? 72 * 1024
-                                           : 110 * 1024;
+  // (the NN stage that carries passive scalars is compiled for two CTAs)
+  const int cap = (dtype == MHD_DTYPE_F64)         ? 200 * 1024
+                  : (recon == RECON_NN && np == 0) ? 72 * 1024
+                                                   : 110 * 1024;
   int best = 4;
   for (int t = 4; t <= (dtype == MHD_DTYPE_F64 ? TileLimits<double>::TMAX
                                                  : TileLimits<float>::TMAX);

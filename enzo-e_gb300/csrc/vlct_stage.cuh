@@ -151,7 +151,9 @@ enum { EXTRA_NONE = 0, EXTRA_FC = 1, EXTRA_ALL = 2 };
 // paths cost a further ~20% of a stage even when idle).
 template <class R, int SOLVER, int RECON, bool DE, int EXTRA>
 __global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
-                                  StageBounds<R, RECON>::min_blocks)
+                                  (EXTRA == EXTRA_ALL && StageBounds<R, RECON>::min_blocks > 2)
+                                      ? 2
+                                      : StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
              const StageTile* __restrict__ tiles, int ntiles, StageInfo info,
              PhysParams phys) {
