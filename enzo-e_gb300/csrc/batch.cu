@@ -295,8 +295,11 @@ int build_descriptors_any(mhdvlct_batch* b, cudaStream_t st) {
                                    : build_descriptors<float>(b, st);
 }
 
-template <class R>
-cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
+// The per-launch scalars of stage s (0: half dt, 1: full dt) of the batch,
+// taking tiles from the work counter `queue`.  Every launch of a stage (the
+// whole-batch launch and the per-group launches of a host-state run) gets
+// its StageInfo here, so none of them can miss an optional term.
+StageInfo batch_stage_info(const mhdvlct_batch* b, int s, int* queue) {
   const StagePlan sp = stage_plan(b->h);
   StageInfo info;
   info.s = sp.s[s];
@@ -305,7 +308,7 @@ cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
   info.dt_factor = sp.dt_factor[s];
   info.tx = b->tile_tx[s];
   info.ty = b->tile_ty[s];
-  info.queue = b->d_queue + s;
+  info.queue = queue;
   info.threads = b->threads[s];
   info.block_fc = (s == 1 && b->fc_on) ? 1 : 0;
   info.fc_g = b->g;
@@ -313,6 +316,13 @@ cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
   // (EnzoMHDIntegratorStageCommands.cpp:279)
   info.gravity = s == 1 ? b->gravity : 0;
   info.npass = b->npass;
+  return info;
+}
+
+template <class R>
+cudaError_t launch_one_stage(mhdvlct_batch* b, int s, cudaStream_t st) {
+  const StagePlan sp = stage_plan(b->h);
+  const StageInfo info = batch_stage_info(b, s, b->d_queue + s);
   return launch_stage<R>(b->h->solver, sp.recon[s], b->h->de != 0,
                          (const StageBlock<R>*)b->d_sblocks[b->parity][s],
                          b->d_tiles[s], b->ntiles[s], info, b->h->phys, b->grid, st);
@@ -960,17 +970,7 @@ int run_host_t(mhdvlct_batch* b, char* host, int ncycles, cudaStream_t st) {
     if (e == cudaSuccess) e = launch_one_stage<R>(b, 0, st);
     const StagePlan sp = stage_plan(b->h);
     for (int g = 0; g < ng && e == cudaSuccess; g++) {
-      StageInfo info;
-      info.s = sp.s[1];
-      info.S = sp.S[1];
-      info.final_stage = 1;
-      info.dt_factor = sp.dt_factor[1];
-      info.tx = b->tile_tx[1];
-      info.ty = b->tile_ty[1];
-      info.queue = b->d_gqueue + g;
-      info.threads = b->threads[1];
-      info.block_fc = b->fc_on ? 1 : 0;
-      info.fc_g = b->g;
+      const StageInfo info = batch_stage_info(b, 1, b->d_gqueue + g);
       e = launch_stage<R>(b->h->solver, sp.recon[1], b->h->de != 0,
                           (const StageBlock<R>*)b->d_sblocks[b->parity][1],
                           b->d_gtiles + b->hg_tile0[g], b->hg_ntile[g], info, b->h->phys,

@@ -316,19 +316,34 @@ def test_zchunked_default_tiles_bit_exact():
         assert np.array_equal(got[k][act], ob.f[ic.ORACLE_NAME[k]][act]), k
 
 
-@pytest.mark.parametrize("ngroups", [1, 3, 8])
-def test_run_host_matches_device_run(ngroups):
+@pytest.mark.parametrize("ngroups,extras", [(1, False), (3, False), (8, False),
+                                            (3, True)])
+def test_run_host_matches_device_run(ngroups, extras):
     """mhdvlct_batch_run_host (state in pinned host memory, copies pipelined
     with the full-dt stage by block groups) gives the same state, bit for
-    bit, as the device-resident graph run of the same cycles."""
+    bit, as the device-resident graph run of the same cycles; with extras,
+    the blocks also carry the acceleration fields and two passive scalars,
+    so the per-group full-dt launches must add the gravity source and
+    advect the scalars exactly as the whole-batch launch does."""
     meth = B.EnzoMethodMHDVlct()
-    nb, N = 2, 24
-    blocks, w = ic.turbulent_box(N=N, nb=nb, g=3, seed=5, mach=1.5)
+    nb, N, g, n = 2, 24, 3, 12
+    blocks, w = ic.turbulent_box(N=N, nb=nb, g=g, seed=5, mach=1.5)
+    if extras:
+        rng = np.random.default_rng(23)
+        m = n + 2 * g
+        act = (slice(g, g + n),) * 3
+        for s in blocks:
+            for k in ("acceleration_x", "acceleration_y", "acceleration_z"):
+                s[k] = np.zeros((m, m, m))
+                s[k][act] = 0.3 * (rng.random((n, n, n)) - 0.5)
+            for k in range(2):
+                s[f"passive_{k}"] = s["density"] * (0.2 + 0.6 * rng.random((m, m, m)))
     nbr = ic.brick_neighbors(nb)
     L = capi.lib()
     runs = []
     for _ in range(2):
-        bt = Batch(meth, [(12, 12, 12)] * 8, [w] * 8, dtype=capi.MHD_DTYPE_F32)
+        bt = Batch(meth, [(n, n, n)] * 8, [w] * 8, dtype=capi.MHD_DTYPE_F32,
+                   npassive=2 if extras else 0, gravity=extras)
         capi.check(L.mhdvlct_batch_set_neighbors(
             bt.h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())))
         for i, s in enumerate(blocks):
@@ -364,6 +379,10 @@ def test_run_host_matches_device_run(ngroups):
         ctypes_cuda_memcpy_raw(want.data_ptr() + off, segp[k], segb[k], to_device=False)
         off += segb[k]
     assert torch.equal(host, want)
+    if extras:
+        # the scalars sit in the state region: the host run advected them
+        got = hst.download(0)
+        assert not np.array_equal(got["passive_0"], blocks[0]["passive_0"].astype(np.float32))
 
 
 def ctypes_cuda_memcpy_raw(dst, src, nbytes, to_device):
