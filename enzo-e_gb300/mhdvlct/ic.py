@@ -226,6 +226,32 @@ def sedov_block(n, g=3, seed=0, e_blast=1.0, sigma_cells=2.0, p0=1e-5,
     return {k: np.ascontiguousarray(v, dtype=dtype) for k, v in blk.items()}, (dx, dx, dx)
 
 
+def amr_block_set(seed=3, counts=((16, 1200), (32, 600), (64, 200)), g=3,
+                  dtype=np.float32):
+    """The mixed-size AMR block set: Sedov blasts (E = 1 in a Gaussian of 2
+    cells at a seeded off-centre point, rho = 1, p = 1e-5,
+    B = (0.05, 0.05, 0.05)) of the given (size, count) pairs, sizes shuffled
+    with the seed; each block's ghost zones come from seeded same-size
+    neighbours.  Returns (blocks, dims, widths, nbr) with nbr the
+    27-neighbour table (entry 13 is the block itself)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.concatenate([np.full(c, n) for n, c in counts])
+    rng.shuffle(sizes)
+    blocks, dims, widths = [], [], []
+    for i, n in enumerate(sizes):
+        blk, w = sedov_block(int(n), g, seed=seed * 7919 + i, width=1.0, dtype=dtype)
+        blk.pop("pressure", None)
+        blocks.append(blk)
+        dims.append((int(n),) * 3)
+        widths.append(w)
+    by_size = {n: np.flatnonzero(sizes == n) for n, _ in counts}
+    nbr = np.empty((len(sizes), 27), dtype=np.int32)
+    for i, n in enumerate(sizes):
+        nbr[i] = rng.choice(by_size[n], size=27)
+        nbr[i, 13] = i
+    return blocks, dims, widths, nbr
+
+
 # oracle field names <-> Cello field names
 ORACLE_NAME = {"density": "rho", "velocity_x": "vx", "velocity_y": "vy",
                "velocity_z": "vz", "total_energy": "etot",

@@ -128,6 +128,9 @@ def lib():
         L.oracle_fill_ghosts_brick.argtypes = [ctypes.POINTER(OracleBlock),
                                                ctypes.c_int, ctypes.c_int,
                                                ctypes.c_int]
+        L.oracle_fill_ghosts_table.argtypes = [ctypes.POINTER(OracleBlock),
+                                               ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_int)]
         L.oracle_ic_inclined_wave.argtypes = [
             ctypes.POINTER(OracleBlock), ctypes.c_char_p, ctypes.c_double,
             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -268,6 +271,17 @@ def fill_ghosts_periodic(b: Block) -> None:
 def fill_ghosts_brick(blocks, nbx, nby, nbz) -> None:
     arr = (OracleBlock * len(blocks))(*[b.cstruct() for b in blocks])
     lib().oracle_fill_ghosts_brick(arr, nbx, nby, nbz)
+
+
+def fill_ghosts_table(blocks, nbr) -> None:
+    """Same-level refresh from a 27-neighbour table (nblocks x 27, entry
+    (sz+1)*9 + (sy+1)*3 + (sx+1) the source of the ghost region at offset
+    (sx, sy, sz)); a block and its neighbours have equal extents."""
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    assert nbr.shape == (len(blocks), 27)
+    arr = (OracleBlock * len(blocks))(*[b.cstruct() for b in blocks])
+    lib().oracle_fill_ghosts_table(arr, len(blocks),
+                                   nbr.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
 
 
 def inclined_wave(b: Block, wave: str, alpha=0.7297276562269663,

@@ -1279,10 +1279,76 @@ void fill_fields(OracleBlock* blocks, int nbx, int nby, int nbz) {
         }
   }
 }
+
+/* The same refresh with the source blocks taken from a 27-neighbour table
+ * instead of a periodic brick: the ghost region at offset (sx, sy, sz) of
+ * block i comes from block nbr[27 i + (sz+1) 9 + (sy+1) 3 + (sx+1)], which
+ * has the same extents as block i (Cello refreshes same-level neighbours of
+ * equal size; the blocks of the table may differ in size from one another).
+ * This is the batch's mhdvlct_batch_set_neighbors refresh. */
+void fill_fields_table(OracleBlock* blocks, int nb, const int* nbr) {
+  const int nfield = 20;
+  for (int f = 0; f < nfield; f++) {
+    int face = -1;
+    if (f == 9) face = 0;
+    if (f == 10) face = 1;
+    if (f == 11) face = 2;
+    auto ptr = [&](OracleBlock& b) -> double* {
+      switch (f) {
+        case 0: return b.rho; case 1: return b.vx; case 2: return b.vy;
+        case 3: return b.vz; case 4: return b.etot; case 5: return b.eint;
+        case 6: return b.bx; case 7: return b.by; case 8: return b.bz;
+        case 9: return b.bfx; case 10: return b.bfy; case 11: return b.bfz;
+        case 12: return b.pressure;
+        case 13: return b.ax; case 14: return b.ay; case 15: return b.az;
+        default: return f - 16 < b.npassive ? b.passive[f - 16] : nullptr;
+      }
+    };
+    if (!ptr(blocks[0])) continue;
+    // sources first, so that the refresh reads pre-refresh values only
+    std::vector<std::vector<double>> snap(nb);
+    auto extent = [&](const OracleBlock& b, int e[3]) {
+      const int g = b.g;
+      e[0] = b.nx + 2 * g + (face == 0);
+      e[1] = b.ny + 2 * g + (face == 1);
+      e[2] = b.nz + 2 * g + (face == 2);
+      return (size_t)e[0] * e[1] * e[2];
+    };
+    for (int ib = 0; ib < nb; ib++) {
+      int e[3];
+      const size_t sz = extent(blocks[ib], e);
+      snap[ib].assign(ptr(blocks[ib]), ptr(blocks[ib]) + sz);
+    }
+    for (int ib = 0; ib < nb; ib++) {
+      OracleBlock& b = blocks[ib];
+      const int g = b.g;
+      const int n[3] = {b.nx, b.ny, b.nz};
+      int e[3];
+      extent(b, e);
+      double* dst = ptr(b);
+      for (int z = 0; z < e[2]; z++)
+        for (int y = 0; y < e[1]; y++)
+          for (int x = 0; x < e[0]; x++) {
+            int sd[3];
+            const int sx = src_index(x, g, n[0], face == 0, &sd[0]);
+            const int sy = src_index(y, g, n[1], face == 1, &sd[1]);
+            const int sz2 = src_index(z, g, n[2], face == 2, &sd[2]);
+            if (sd[0] == 0 && sd[1] == 0 && sd[2] == 0) continue;
+            const int sb = nbr[27 * (size_t)ib + (sd[2] + 1) * 9 + (sd[1] + 1) * 3 + (sd[0] + 1)];
+            dst[((size_t)z * e[1] + y) * e[0] + x] =
+                snap[sb][((size_t)sz2 * e[1] + sy) * e[0] + sx];
+          }
+    }
+  }
+}
 }  // namespace
 
 extern "C" void oracle_fill_ghosts_periodic(OracleBlock* b) {
   fill_fields(b, 1, 1, 1);
+}
+
+extern "C" void oracle_fill_ghosts_table(OracleBlock* blocks, int nb, const int* nbr) {
+  fill_fields_table(blocks, nb, nbr);
 }
 
 extern "C" void oracle_fill_ghosts_brick(OracleBlock* blocks, int nbx, int nby,
