@@ -412,6 +412,151 @@ int cuda_fail(mhdvlct_handle* h, cudaError_t e, const char* where) {
   return fail(h, MHD_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// Descriptor uploads go through a kernel parameter instead of a
+// cudaMemcpyAsync from host memory: a copy from pageable memory may make the
+// host wait for the stream, so consecutive per-block calls would no longer
+// queue behind each other.  The bytes are passed by value in chunks.
+constexpr int kBlobBytes = 1024;
+struct Blob {
+  unsigned char b[kBlobBytes];
+};
+__global__ void put_blob_kernel(unsigned char* dst, Blob src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src.b[i];
+}
+cudaError_t put_bytes(void* dst, const void* src, size_t n, cudaStream_t st) {
+  const unsigned char* s = (const unsigned char*)src;
+  for (size_t off = 0; off < n; off += kBlobBytes) {
+    const int k = (int)std::min<size_t>(kBlobBytes, n - off);
+    Blob bl;
+    std::memcpy(bl.b, s + off, k);
+    put_blob_kernel<<<1, 128, 0, st>>>((unsigned char*)dst + off, bl, k);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Cello's min-reduction of the blocks' dt (control_stopping.cpp:96-106) on
+// the device: one CTA, a min is exact in any order.
+__global__ void dt_min_kernel(const double* v, int n, double* out) {
+  __shared__ double red[256];
+  double m = v[0];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = (v[i] < m) ? v[i] : m;
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      const double o = red[threadIdx.x + w];
+      if (o < red[threadIdx.x]) red[threadIdx.x] = o;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+cudaError_t launch_dt_min(const double* v, int n, double* out, cudaStream_t st) {
+  dt_min_kernel<<<1, 256, 0, st>>>(v, n, out);
+  return cudaGetLastError();
+}
+
+// The tiles of make_tiles (same near-equal split of each axis, same order:
+// x fastest, then y, then z), generated on the device: tile i of
+// nx * ny * nz parts of the output window [lo, hi_a) of each axis a.
+struct TileSplit {
+  int block, lo, len[3], np[3];
+};
+__global__ void make_tiles_kernel(StageTile* out, TileSplit sp) {
+  const int n = sp.np[0] * sp.np[1] * sp.np[2];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    int q[3] = {t % sp.np[0], (t / sp.np[0]) % sp.np[1], t / (sp.np[0] * sp.np[1])};
+    int a0[3], a1[3];
+    for (int a = 0; a < 3; a++) {
+      const int base = sp.len[a] / sp.np[a], rem = sp.len[a] % sp.np[a];
+      a0[a] = sp.lo + q[a] * base + (q[a] < rem ? q[a] : rem);
+      a1[a] = a0[a] + base + (q[a] < rem ? 1 : 0);
+    }
+    out[t] = StageTile{sp.block, a0[0], a1[0], a0[1], a1[1], a0[2], a1[2]};
+  }
+}
+// The split of one stage's output window into tiles of at most tx x ty
+// columns and z-chunks of zchunk planes (0: whole window); ntiles() = 0 when
+// the window is empty.
+TileSplit tile_split(const int m[3], int S, bool final, int tx, int ty, int zchunk) {
+  TileSplit sp{};
+  sp.lo = final ? S : S + 1;
+  const int t[3] = {tx, ty, zchunk};
+  for (int a = 0; a < 3; a++) {
+    sp.len[a] = (final ? m[a] - S : m[a] - S - 1) - sp.lo;
+    int ta = t[a];
+    if (sp.len[a] <= 0) {
+      sp.np[0] = sp.np[1] = sp.np[2] = 0;
+      return sp;
+    }
+    if (ta <= 0 || ta > sp.len[a]) ta = sp.len[a];
+    sp.np[a] = (sp.len[a] + ta - 1) / ta;
+  }
+  return sp;
+}
+long ntiles_of(const TileSplit& sp) { return (long)sp.np[0] * sp.np[1] * sp.np[2]; }
+cudaError_t launch_make_tiles(StageTile* out, const TileSplit& sp, cudaStream_t st) {
+  const long n = ntiles_of(sp);
+  if (n <= 0) return cudaSuccess;
+  make_tiles_kernel<<<(int)std::min<long>((n + 127) / 128, 64), 128, 0, st>>>(out, sp);
+  return cudaGetLastError();
+}
+
+// Work decomposition of one stage of the per-block path: the tile extent and
+// z-chunk that minimise a simple cost model for one block alone on the GPU.
+// A tile of t x t columns and L planes costs about (t+2)^2 (L + 1.5) (its
+// halo columns and the planes of its prologue); the tiles run in waves of
+// the CTAs the GPU holds at once (one per SM for FP64, two or three for
+// FP32), so the stage takes about waves x the largest tile's cost.
+struct PlainDecomp {
+  int tile[2] = {8, 8};
+  int zchunk[2] = {0, 0};
+};
+int sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = 1;
+    return v;
+  }();
+  return n;
+}
+PlainDecomp plain_decomp(const mhdvlct_handle* h, const int m[3], int dtype, int np) {
+  PlainDecomp d;
+  const StagePlan sp = stage_plan(h);
+  for (int i = 0; i < sp.nstages; i++) {
+    const bool final = i + 1 == sp.nstages;
+    const int tmax = default_tile(dtype, h->solver, sp.recon[i], h->de, np);
+    const int per_sm = dtype == MHD_DTYPE_F64 ? 1
+                       : (sp.recon[i] == RECON_NN && np == 0) ? 3 : 2;
+    const long resident = (long)per_sm * sm_count();
+    double best = 1e300;
+    for (int t = std::min(6, tmax); t <= tmax; t++) {
+      for (int L : {0, 16, 12, 8, 6, 4}) {
+        const TileSplit s = tile_split(m, sp.S[i], final, t, t, L);
+        const long n = ntiles_of(s);
+        if (n <= 0) continue;
+        const int tx = (s.len[0] + s.np[0] - 1) / s.np[0];
+        const int ty = (s.len[1] + s.np[1] - 1) / s.np[1];
+        const int tz = (s.len[2] + s.np[2] - 1) / s.np[2];
+        const double cost = (double)((n + resident - 1) / resident) * (tx + 2) * (ty + 2) *
+                            (tz + 1.5);
+        if (cost < best * 0.999) {  // on ties the smaller tile / fewer chunks stays
+          best = cost;
+          d.tile[i] = t;
+          d.zchunk[i] = L;
+        }
+      }
+    }
+    if (h->tile > 0) d.tile[i] = h->tile;  // a tile set on the handle wins
+    if (h->zchunk > 0) d.zchunk[i] = h->zchunk;
+  }
+  return d;
+}
+
 // Scratch of the plain path, carved from one allocation.
 template <class R> struct PlainScratch {
   R* tmp[NCELL];
@@ -427,6 +572,7 @@ template <class R> struct PlainScratch {
   void* d_fc;                // FluxOut<R> for the boundary fluxes
   StageTile* d_tiles;        // stage 0 tiles then stage 1 tiles
   int ntiles[2];
+  int tile[2];               // largest tile extent of each stage
 };
 
 size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -435,11 +581,13 @@ template <class R>
 int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
                    PlainScratch<R>& S, cudaStream_t st, int np = 0) {
   const StagePlan sp = stage_plan(h);
-  if (h->tile <= 0) h->tile = 8;
-  std::vector<StageTile> tiles[2];
-  for (int i = 0; i < sp.nstages; i++)
-    make_tiles(0, m, sp.S[i], i + 1 == sp.nstages, h->tile, h->tile, h->zchunk,
-               tiles[i]);
+  const PlainDecomp dc = plain_decomp(h, m, dtype, np);
+  TileSplit ts[2] = {};
+  long nt[2] = {0, 0};
+  for (int i = 0; i < sp.nstages; i++) {
+    ts[i] = tile_split(m, sp.S[i], i + 1 == sp.nstages, dc.tile[i], dc.tile[i], dc.zchunk[i]);
+    nt[i] = ntiles_of(ts[i]);
+  }
   const size_t M = (size_t)m[0] * m[1] * m[2];
   const size_t F[3] = {(size_t)(m[0] + 1) * m[1] * m[2],
                        (size_t)m[0] * (m[1] + 1) * m[2],
@@ -458,7 +606,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   take(sizeof(AuxBlock<R>));
   take(27 * sizeof(int));
   take(sizeof(FluxOut<R>));
-  take((tiles[0].size() + tiles[1].size()) * sizeof(StageTile));
+  take((size_t)(nt[0] + nt[1]) * sizeof(StageTile));
   const bool same = h->scratch && h->cache_dtype == dtype && h->cache_m[0] == m[0] &&
                     h->cache_m[1] == m[1] && h->cache_m[2] == m[2] &&
                     h->cache_np == np && h->scratch_bytes >= off;
@@ -492,17 +640,17 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   S.d_nbr = (int*)(base + offs[i++]);
   S.d_fc = (void*)(base + offs[i++]);
   S.d_tiles = (StageTile*)(base + offs[i++]);
-  S.ntiles[0] = (int)tiles[0].size();
-  S.ntiles[1] = (int)tiles[1].size();
+  S.ntiles[0] = (int)nt[0];
+  S.ntiles[1] = (int)nt[1];
+  S.tile[0] = dc.tile[0];
+  S.tile[1] = dc.tile[1];
   if (!same) {
-    std::vector<StageTile> all(tiles[0]);
-    all.insert(all.end(), tiles[1].begin(), tiles[1].end());
-    cudaError_t e = cudaMemcpyAsync(S.d_tiles, all.data(), all.size() * sizeof(StageTile),
-                                    cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "tile upload");
-    std::vector<int> nbr(27, 0);
-    e = cudaMemcpyAsync(S.d_nbr, nbr.data(), 27 * sizeof(int), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "neighbour upload");
+    cudaError_t e = launch_make_tiles(S.d_tiles, ts[0], st);
+    if (e == cudaSuccess) e = launch_make_tiles(S.d_tiles + nt[0], ts[1], st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "tile set-up");
+    // a single block refreshes from itself: every neighbour entry is 0
+    e = cudaMemsetAsync(S.d_nbr, 0, 27 * sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "neighbour set-up");
     // scratch cell fields that a block never writes must still be defined
     e = cudaMemsetAsync(h->scratch, 0, offs[NCELL + 6 + np], st);
     if (e != cudaSuccess) return cuda_fail(h, e, "scratch clear");
@@ -510,23 +658,23 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   return MHD_OK;
 }
 
+// One block step on scratch S, whose tiles are in place: the stage
+// descriptors, the euler copy, both stages and the face copy-back.  dt is
+// read on the device from d_dt.  Shared by the allocating and the
+// no-allocation entry points.
 template <class R>
-int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
-                 const MhdFluxCorrection* fc, cudaStream_t st) {
+int block_step_on(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
+                  const double* d_dt, const MhdFluxCorrection* fc, cudaStream_t st) {
   const int g = b->ghost[0];
   const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
-  PlainScratch<R> S;
   const int np = b->npassive;
-  int rc = ensure_scratch<R>(h, m, b->dtype, S, st, np);
-  if (rc) return rc;
   const StagePlan sp = stage_plan(h);
   FieldSet<R> ext = fieldset_of<R>(b);
   FieldSet<R> tmp;
   for (int k = 0; k < NCELL; k++) tmp.c[k] = S.tmp[k];
   for (int d = 0; d < 3; d++) tmp.f[d] = S.tface[d];
   const size_t M = (size_t)m[0] * m[1] * m[2];
-  cudaError_t e = launch_set_scalar(S.d_dt, dt, st);
-  if (e != cudaSuccess) return cuda_fail(h, e, "dt upload");
+  cudaError_t e;
 
   StageBlock<R> sb[2];
   for (int i = 0; i < sp.nstages; i++) {
@@ -535,7 +683,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
       B.m[a] = m[a];
       B.cw[a] = b->cell_width[a];
     }
-    B.dt = S.d_dt;
+    B.dt = d_dt;
     const bool final = (i + 1) == sp.nstages;
     B.base = ext;
     for (int d = 0; d < 3; d++) B.accel[d] = (const R*)b->acceleration[d];
@@ -565,7 +713,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
       for (int d = 0; d < 3; d++) B.out.f[d] = S.fface[d];
     }
   }
-  e = cudaMemcpyAsync(S.d_sblocks, sb, sizeof(sb), cudaMemcpyHostToDevice, st);
+  e = put_bytes(S.d_sblocks, sb, sizeof(sb), st);
   if (e != cudaSuccess) return cuda_fail(h, e, "block upload");
   if (fc) {
     FluxOut<R> fo;
@@ -573,7 +721,7 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
       for (int sd = 0; sd < 2; sd++)
         for (int q = 0; q < 6; q++) fo.f[d][sd][q] = (R*)fc->flux[d][sd][q];
     fo.g = b->ghost[0];
-    e = cudaMemcpyAsync(S.d_fc, &fo, sizeof(fo), cudaMemcpyHostToDevice, st);
+    e = put_bytes(S.d_fc, &fo, sizeof(fo), st);
     if (e != cudaSuccess) return cuda_fail(h, e, "flux buffer upload");
   }
   if (sp.nstages == 1) {
@@ -595,8 +743,8 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     info.S = sp.S[i];
     info.final_stage = (i + 1) == sp.nstages;
     info.dt_factor = sp.dt_factor[i];
-    info.tx = h->tile;
-    info.ty = h->tile;
+    info.tx = S.tile[i];
+    info.ty = S.tile[i];
     info.queue = nullptr;
     info.threads = 256;
     // EnzoMHDIntegratorStageCommands.cpp:279: the gravity source enters the
@@ -620,6 +768,24 @@ int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   return MHD_OK;
 }
 
+// The allocating block step: dt from the host (d_dt null) or from device
+// memory (d_dt).
+template <class R>
+int block_step_t(mhdvlct_handle* h, const MhdBlockView* b, double dt, const double* d_dt,
+                 const MhdFluxCorrection* fc, cudaStream_t st) {
+  const int g = b->ghost[0];
+  const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
+  PlainScratch<R> S;
+  int rc = ensure_scratch<R>(h, m, b->dtype, S, st, b->npassive);
+  if (rc) return rc;
+  if (!d_dt) {
+    cudaError_t e = launch_set_scalar(S.d_dt, dt, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "dt upload");
+    d_dt = S.d_dt;
+  }
+  return block_step_on<R>(h, b, S, d_dt, fc, st);
+}
+
 template <class R>
 int aux_setup(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
               cudaStream_t st) {
@@ -636,14 +802,16 @@ int aux_setup(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
   a.pressure = (R*)b->pressure;
   for (int k = 0; k < b->npassive; k++) a.pass[k] = (R*)b->passive[k];
   for (int d = 0; d < 3; d++) a.accel[d] = (R*)b->acceleration[d];
-  cudaError_t e = cudaMemcpyAsync(S.d_aux, &a, sizeof(a), cudaMemcpyHostToDevice, st);
+  cudaError_t e = put_bytes(S.d_aux, &a, sizeof(a), st);
   if (e != cudaSuccess) return cuda_fail(h, e, "aux upload");
   return MHD_OK;
 }
 
+// EnzoMethodMHDVlct::timestep into device memory (d_dt_out), or, with
+// d_dt_out null, returned in *dt_out after a stream synchronisation.
 template <class R>
 int block_timestep_t(mhdvlct_handle* h, const MhdBlockView* b, double* dt_out,
-                     cudaStream_t st) {
+                     double* d_dt_out, cudaStream_t st) {
   PlainScratch<R> S;
   int rc = aux_setup<R>(h, b, S, st);
   if (rc) return rc;
@@ -651,8 +819,10 @@ int block_timestep_t(mhdvlct_handle* h, const MhdBlockView* b, double* dt_out,
   const size_t M = (size_t)(b->n[0] + 2 * g) * (b->n[1] + 2 * g) * (b->n[2] + 2 * g);
   const int chunks = (int)std::min<size_t>(std::max<size_t>(1, M / 1024), 1024);
   cudaError_t e = launch_timestep<R>(h->mhd != 0, h->de != 0, S.d_aux, 1, chunks, h->phys,
-                                     S.d_smax, h->params.courant, 0, S.d_dtout, nullptr, st);
+                                     S.d_smax, h->params.courant, 0,
+                                     d_dt_out ? d_dt_out : S.d_dtout, nullptr, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "timestep launch");
+  if (d_dt_out) return MHD_OK;
   e = cudaMemcpyAsync(dt_out, S.d_dtout, sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "dt download");
   e = cudaStreamSynchronize(st);
@@ -681,8 +851,8 @@ extern "C" int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b,
   if (rc) return rc;
   if (!(dt > 0) || !std::isfinite(dt)) return fail(h, MHD_ERR_INVALID, "dt must be positive and finite");
   cudaStream_t st = (cudaStream_t)stream;
-  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, nullptr, st)
-                                   : block_step_t<float>(h, b, dt, nullptr, st);
+  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, nullptr, nullptr, st)
+                                   : block_step_t<float>(h, b, dt, nullptr, nullptr, st);
 }
 
 extern "C" int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, double dt,
@@ -700,8 +870,8 @@ extern "C" int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, d
       if (fc->flux[d][sd][MHD_Q_INTERNAL_ENERGY] && !h->de)
         return fail(h, MHD_ERR_INVALID, "internal_energy fluxes need dual energy");
   cudaStream_t st = (cudaStream_t)stream;
-  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, fc, st)
-                                   : block_step_t<float>(h, b, dt, fc, st);
+  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, nullptr, fc, st)
+                                   : block_step_t<float>(h, b, dt, nullptr, fc, st);
 }
 
 extern "C" int mhdvlct_block_bfield_from_potential(mhdvlct_handle* h, const MhdBlockView* b,
@@ -735,8 +905,35 @@ extern "C" int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
   int rc = check_view(h, b);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  return b->dtype == MHD_DTYPE_F64 ? block_timestep_t<double>(h, b, dt_out, st)
-                                   : block_timestep_t<float>(h, b, dt_out, st);
+  return b->dtype == MHD_DTYPE_F64 ? block_timestep_t<double>(h, b, dt_out, nullptr, st)
+                                   : block_timestep_t<float>(h, b, dt_out, nullptr, st);
+}
+
+extern "C" int mhdvlct_block_timestep_device(mhdvlct_handle* h, const MhdBlockView* b,
+                                             double* dt_dev, void* stream) {
+  if (!h || !dt_dev) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? block_timestep_t<double>(h, b, nullptr, dt_dev, st)
+                                   : block_timestep_t<float>(h, b, nullptr, dt_dev, st);
+}
+
+extern "C" int mhdvlct_block_step_device_dt(mhdvlct_handle* h, const MhdBlockView* b,
+                                            const double* dt_dev, void* stream) {
+  if (!h || !dt_dev) return MHD_ERR_INVALID;
+  int rc = check_view(h, b);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, 0.0, dt_dev, nullptr, st)
+                                   : block_step_t<float>(h, b, 0.0, dt_dev, nullptr, st);
+}
+
+extern "C" int mhdvlct_dt_min_device(mhdvlct_handle* h, const double* dt_dev, int n,
+                                     double* dt_min_dev, void* stream) {
+  if (!h || !dt_dev || !dt_min_dev || n <= 0) return MHD_ERR_INVALID;
+  cudaError_t e = launch_dt_min(dt_dev, n, dt_min_dev, (cudaStream_t)stream);
+  return e == cudaSuccess ? MHD_OK : cuda_fail(h, e, "dt min");
 }
 
 extern "C" int mhdvlct_fill_ghosts_periodic(mhdvlct_handle* h, const MhdBlockView* b,
@@ -758,7 +955,7 @@ extern "C" int mhdvlct_fill_ghosts_periodic(mhdvlct_handle* h, const MhdBlockVie
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB per device
-constexpr int kNoAllocMaxTiles = 512;                     // per stage
+constexpr int kNoAllocMaxTiles = 1024;                    // per stage
 constexpr int kNoAllocMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -785,63 +982,30 @@ int noalloc_base(mhdvlct_handle* h, char** out) {
   return MHD_OK;
 }
 
-// The tiles make_tiles produces (same order, same near-equal split), written
-// into a caller array of capacity `cap`; returns the count, or -1 past cap.
-int noalloc_tiles(const int m[3], int S, bool final, int tx, int ty, int zchunk,
-                  StageTile* out, int cap) {
-  const int lo = final ? S : S + 1;
-  const int hi[3] = {final ? m[0] - S : m[0] - S - 1, final ? m[1] - S : m[1] - S - 1,
-                     final ? m[2] - S : m[2] - S - 1};
-  int len[3], t[3] = {tx, ty, 0}, np[3];
-  t[2] = zchunk > 0 ? zchunk : (hi[2] - lo);
-  for (int a = 0; a < 3; a++) {
-    len[a] = hi[a] - lo;
-    if (len[a] <= 0) return 0;
-    if (t[a] <= 0 || t[a] > len[a]) t[a] = len[a];
-    np[a] = (len[a] + t[a] - 1) / t[a];
-  }
-  if ((long long)np[0] * np[1] * np[2] > cap) return -1;
-  auto part = [&](int a, int i, int& p0, int& p1) {
-    p0 = lo;
-    for (int j = 0; j < i; j++) p0 += len[a] / np[a] + (j < len[a] % np[a] ? 1 : 0);
-    p1 = p0 + len[a] / np[a] + (i < len[a] % np[a] ? 1 : 0);
-  };
-  int n = 0;
-  for (int k = 0; k < np[2]; k++)
-    for (int j = 0; j < np[1]; j++)
-      for (int i = 0; i < np[0]; i++) {
-        StageTile& T = out[n++];
-        T.block = 0;
-        part(0, i, T.xa, T.xb);
-        part(1, j, T.ya, T.yb);
-        part(2, k, T.za, T.zb);
-      }
-  return n;
-}
-
 template <class R>
 int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
                          cudaStream_t st) {
   const int g = b->ghost[0];
   const int m[3] = {b->n[0] + 2 * g, b->n[1] + 2 * g, b->n[2] + 2 * g};
   const StagePlan sp = stage_plan(h);
-  if (h->tile <= 0) h->tile = 8;
-
-  // the tile lists live on the host stack, bounded by kNoAllocMaxTiles
-  StageTile tiles[2][kNoAllocMaxTiles];
-  int ntiles[2] = {0, 0};
+  const int np = b->npassive;
+  // the same work decomposition as mhdvlct_block_step
+  const PlainDecomp dc = plain_decomp(h, m, b->dtype, np);
+  TileSplit ts[2] = {};
+  long nt[2] = {0, 0};
   for (int i = 0; i < sp.nstages; i++) {
-    ntiles[i] = noalloc_tiles(m, sp.S[i], i + 1 == sp.nstages, h->tile, h->tile,
-                              h->zchunk, tiles[i], kNoAllocMaxTiles);
-    if (ntiles[i] < 0)
+    ts[i] = tile_split(m, sp.S[i], i + 1 == sp.nstages, dc.tile[i], dc.tile[i], dc.zchunk[i]);
+    nt[i] = ntiles_of(ts[i]);
+    if (nt[i] > kNoAllocMaxTiles)
       return fail(h, MHD_ERR_INVALID,
                   "block needs more than " + std::to_string(kNoAllocMaxTiles) +
                       " tiles per stage; mhdvlct_block_step_noalloc cannot take it "
                       "(use mhdvlct_block_step)");
   }
 
-  // carve the static array: cells, stage-0 faces, final faces, dt, stage
-  // descriptors, tiles (each region 256-byte aligned)
+  // carve the static array: cells, half-step scalars, stage-0 faces, final
+  // faces, dt, stage descriptors, flux-output record, tiles (each region
+  // 256-byte aligned)
   const size_t M = (size_t)m[0] * m[1] * m[2];
   const size_t F[3] = {(size_t)(m[0] + 1) * m[1] * m[2], (size_t)m[0] * (m[1] + 1) * m[2],
                        (size_t)m[0] * m[1] * (m[2] + 1)};
@@ -852,14 +1016,13 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     return o;
   };
   size_t o_tmp[NCELL], o_tf[3], o_ff[3], o_tp[4];
-  const int np = b->npassive;
   for (int k = 0; k < NCELL; k++) o_tmp[k] = take(M * sizeof(R));
   for (int k = 0; k < np; k++) o_tp[k] = take(M * sizeof(R));  // half-step scalars
   for (int d = 0; d < 3; d++) o_tf[d] = take(F[d] * sizeof(R));
   for (int d = 0; d < 3; d++) o_ff[d] = take(F[d] * sizeof(R));
   const size_t o_dt = take(sizeof(double));
   const size_t o_sb = take(2 * sizeof(StageBlock<R>));
-  const size_t o_tl = take((size_t)(ntiles[0] + ntiles[1]) * sizeof(StageTile));
+  const size_t o_tl = take((size_t)(nt[0] + nt[1]) * sizeof(StageTile));
   if (off > kNoAllocScratchBytes)
     return fail(h, MHD_ERR_INVALID,
                 "block needs " + std::to_string(off) +
@@ -870,7 +1033,7 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   char* base = nullptr;
   int rc = noalloc_base(h, &base);
   if (rc) return rc;
-  PlainScratch<R> S;
+  PlainScratch<R> S{};
   for (int k = 0; k < NCELL; k++) S.tmp[k] = (R*)(base + o_tmp[k]);
   for (int k = 0; k < 4; k++) S.tpass[k] = k < np ? (R*)(base + o_tp[k]) : nullptr;
   for (int d = 0; d < 3; d++) {
@@ -880,96 +1043,17 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   S.d_dt = (double*)(base + o_dt);
   S.d_sblocks = (StageBlock<R>*)(base + o_sb);
   S.d_tiles = (StageTile*)(base + o_tl);
-
-  FieldSet<R> ext = fieldset_of<R>(b);
-  FieldSet<R> tmp;
-  for (int k = 0; k < NCELL; k++) tmp.c[k] = S.tmp[k];
-  for (int d = 0; d < 3; d++) tmp.f[d] = S.tface[d];
+  S.ntiles[0] = (int)nt[0];
+  S.ntiles[1] = (int)nt[1];
+  S.tile[0] = dc.tile[0];
+  S.tile[1] = dc.tile[1];
+  // every call rewrites the dt slot, the descriptors and the tile lists (the
+  // array keeps whatever the previous call left)
   cudaError_t e = launch_set_scalar(S.d_dt, dt, st);
-  if (e != cudaSuccess) return cuda_fail(h, e, "dt upload");
-
-  StageBlock<R> sb[2];
-  for (int i = 0; i < sp.nstages; i++) {
-    StageBlock<R>& B = sb[i];
-    for (int a = 0; a < 3; a++) {
-      B.m[a] = m[a];
-      B.cw[a] = b->cell_width[a];
-    }
-    B.dt = S.d_dt;
-    B.base = ext;
-    for (int d = 0; d < 3; d++) B.accel[d] = (const R*)b->acceleration[d];
-    for (int k = 0; k < np; k++) {
-      // as mhdvlct_block_step: vl writes the half step into scratch and then
-      // the caller's scalars; euler reads a copy (made below)
-      R* ep = (R*)b->passive[k];
-      B.pass_base[k] = ep;
-      B.pass_cur[k] = (sp.nstages == 1 || i == 1) ? S.tpass[k] : ep;
-      B.pass_out[k] = (sp.nstages == 2 && i == 0) ? S.tpass[k] : ep;
-    }
-    if (sp.nstages == 1) {
-      B.cur = tmp;
-      for (int d = 0; d < 3; d++) B.cur.f[d] = ext.f[d];
-      B.out = ext;
-    } else if (i == 0) {
-      B.cur = ext;
-      B.out = tmp;
-    } else {
-      B.cur = tmp;
-      B.out = ext;
-    }
-    if (i + 1 == sp.nstages)
-      for (int d = 0; d < 3; d++) B.out.f[d] = S.fface[d];
-  }
-  e = cudaMemcpyAsync(S.d_sblocks, sb, sizeof(sb), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_fail(h, e, "block upload");
-  if (ntiles[0] > 0) {
-    e = cudaMemcpyAsync(S.d_tiles, tiles[0], ntiles[0] * sizeof(StageTile),
-                        cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "tile upload");
-  }
-  if (ntiles[1] > 0) {
-    e = cudaMemcpyAsync(S.d_tiles + ntiles[0], tiles[1], ntiles[1] * sizeof(StageTile),
-                        cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "tile upload");
-  }
-  if (sp.nstages == 1) {
-    for (int k = 0; k < NCELL; k++) {
-      if (!ext.c[k]) continue;
-      e = cudaMemcpyAsync(S.tmp[k], ext.c[k], M * sizeof(R), cudaMemcpyDeviceToDevice, st);
-      if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
-    }
-    for (int k = 0; k < np; k++) {
-      e = cudaMemcpyAsync(S.tpass[k], b->passive[k], M * sizeof(R), cudaMemcpyDeviceToDevice,
-                          st);
-      if (e != cudaSuccess) return cuda_fail(h, e, "euler copy");
-    }
-  }
-  const StageTile* dtiles[2] = {S.d_tiles, S.d_tiles + ntiles[0]};
-  for (int i = 0; i < sp.nstages; i++) {
-    StageInfo info;
-    info.s = sp.s[i];
-    info.S = sp.S[i];
-    info.final_stage = (i + 1) == sp.nstages;
-    info.dt_factor = sp.dt_factor[i];
-    info.tx = h->tile;
-    info.ty = h->tile;
-    info.queue = nullptr;
-    info.threads = 256;
-    // EnzoMHDIntegratorStageCommands.cpp:279: the gravity source enters the
-    // stage with index 1 (the full-dt stage of vl; never with euler)
-    info.gravity = (i == 1 && b->acceleration[0] != nullptr) ? 1 : 0;
-    info.npass = np;
-    e = launch_stage<R>(h->solver, sp.recon[i], h->de != 0, S.d_sblocks + i, dtiles[i],
-                        ntiles[i], info, h->phys, 0, st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "stage launch");
-  }
-  if (h->mhd) {
-    const int S1 = sp.S[sp.nstages - 1] + 1;
-    e = launch_copy_faces<R>(m[0], m[1], m[2], S1, S.fface[0], S.fface[1], S.fface[2],
-                             ext.f[0], ext.f[1], ext.f[2], st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "face copy");
-  }
-  return MHD_OK;
+  if (e == cudaSuccess) e = launch_make_tiles(S.d_tiles, ts[0], st);
+  if (e == cudaSuccess) e = launch_make_tiles(S.d_tiles + nt[0], ts[1], st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "no-alloc set-up");
+  return block_step_on<R>(h, b, S, S.d_dt, nullptr, st);
 }
 
 }  // namespace

@@ -31,6 +31,8 @@ EXPORTED = (
     "mhdvlct_block_step_noalloc", "mhdvlct_block_step_fc",
     "mhdvlct_block_bfield_from_potential",
     "mhdvlct_block_timestep", "mhdvlct_fill_ghosts_periodic",
+    "mhdvlct_block_timestep_device", "mhdvlct_dt_min_device",
+    "mhdvlct_block_step_device_dt",
     "mhdvlct_refresh_faces", "mhdvlct_refresh_face_box", "mhdvlct_flux_correct",
     "mhdvlct_batch_create", "mhdvlct_batch_create_ex", "mhdvlct_batch_destroy",
     "mhdvlct_batch_block_view", "mhdvlct_batch_set_neighbors",
@@ -145,6 +147,9 @@ def lib() -> ctypes.CDLL:
     L.mhdvlct_block_bfield_from_potential.argtypes = [vp, P(MhdBlockView), vp, vp, vp, vp]
     L.mhdvlct_block_timestep.argtypes = [vp, P(MhdBlockView), P(dp), vp]
     L.mhdvlct_fill_ghosts_periodic.argtypes = [vp, P(MhdBlockView), vp]
+    L.mhdvlct_block_timestep_device.argtypes = [vp, P(MhdBlockView), vp, vp]
+    L.mhdvlct_dt_min_device.argtypes = [vp, vp, ip, vp, vp]
+    L.mhdvlct_block_step_device_dt.argtypes = [vp, P(MhdBlockView), vp, vp]
     L.mhdvlct_refresh_faces.argtypes = [vp, P(MhdBlockView), ip, P(MhdRefreshFace), ip,
                                         ctypes.c_uint, vp]
     L.mhdvlct_refresh_face_box.argtypes = [P(ip)] * 3 + [ip] + [P(ip)] * 6

@@ -153,6 +153,24 @@ int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, double dt,
 int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
                            double* dt_out, void* stream);
 
+/* The timestep, the dt reduction and the step with dt kept on the device, so
+ * that a process driving many blocks through the per-block calls never waits
+ * for the GPU inside a cycle: each block's dt goes to a device slot
+ * (EnzoMethodMHDVlct::timestep, EnzoMethodMHDVlct.cpp:551-588), one call
+ * takes the minimum over the slots (Cello's min-reduction over blocks,
+ * src/Cello/control_stopping.cpp:96-106), and every block's step reads that
+ * minimum on the device (EnzoMethodMHDVlct::compute with block->dt(),
+ * EnzoMethodMHDVlct.cpp:356-500).  All three only enqueue work on `stream`;
+ * dt_dev / dt_min_dev are device pointers to doubles owned by the caller.
+ * The step does not check the dt it reads: it must be positive and finite
+ * when the step runs. */
+int mhdvlct_block_timestep_device(mhdvlct_handle* h, const MhdBlockView* b,
+                                  double* dt_dev, void* stream);
+int mhdvlct_dt_min_device(mhdvlct_handle* h, const double* dt_dev, int n,
+                          double* dt_min_dev, void* stream);
+int mhdvlct_block_step_device_dt(mhdvlct_handle* h, const MhdBlockView* b,
+                                 const double* dt_dev, void* stream);
+
 /* No counterpart in the reference (the reference's compute allocates its
  * scratch through EnzoVlctScratchSpace on the host heap).  Same operation and
  * results as mhdvlct_block_step, but allocates no device memory: its scratch
@@ -162,7 +180,7 @@ int mhdvlct_block_timestep(mhdvlct_handle* h, const MhdBlockView* b,
  * capture.  A block whose scratch (all cell fields, the passive scalars'
  * half step and two sets of face fields at the ghosted extents, plus
  * descriptors) exceeds 8 MiB, or whose
- * stage needs more than 512 tiles, is rejected with MHD_ERR_INVALID and a
+ * stage needs more than 1024 tiles, is rejected with MHD_ERR_INVALID and a
  * message naming the bytes needed (an FP64 block of 32^3 cells with 3 ghost
  * zones needs about 6.7 MB).  Nothing in the array has to start at zero:
  * every call rewrites the dt slot, the stage descriptors and the tile list,

@@ -149,3 +149,62 @@ def test_invalid_arguments_are_rejected():
     blk = B.Block(8, 2, (0.1, 0.1, 0.1))  # ghost depth 2 < 3
     with pytest.raises(Exception):
         meth.compute(blk, 0.01)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_device_dt_cycle_matches_oracle(dtype):
+    """The per-block calls with dt kept on the device: every block's dt into
+    a device slot, the device min over the slots, each block stepped with
+    that min read on the device -- the same cycle as Cello's (timestep per
+    block, global min, refresh, step) without any host synchronisation.
+    FP64 is bit-exact against the oracle (dt included); FP32 is within 1e-5
+    and equals the same calls with the dt passed from the host."""
+    from mhdvlct import capi
+    import ctypes
+    L = capi.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    sizes = [(8, 6, 7), (12, 10, 9), (32, 32, 32)]
+    meth = B.EnzoMethodMHDVlct()
+    blks, obs, twins = [], [], []
+    for i, n in enumerate(sizes):
+        state, w = ic.smooth_block(n, 3, seed=60 + i)
+        for lst in (blks, twins):
+            b = B.Block(n, 3, w, dtype=dtype)
+            b.load_numpy(state)
+            lst.append(b)
+        obs.append(oracle_block(state, n, 3, w))
+    prm = oracle_params(courant=meth.courant)
+    slots = torch.zeros(len(sizes), dtype=torch.float64, device="cuda")
+    dmin = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        views = [b.view() for b in blks]
+        for i, v in enumerate(views):
+            capi.check(L.mhdvlct_block_timestep_device(
+                meth.handle, ctypes.byref(v), slots.data_ptr() + 8 * i, st), meth.handle)
+        capi.check(L.mhdvlct_dt_min_device(meth.handle, slots.data_ptr(), len(sizes),
+                                           dmin.data_ptr(), st), meth.handle)
+        for b, v in zip(blks, views):
+            meth.fill_ghosts_periodic(b)
+            capi.check(L.mhdvlct_block_step_device_dt(meth.handle, ctypes.byref(v),
+                                                      dmin.data_ptr(), st), meth.handle)
+        # the same cycle through the host-dt calls
+        dt_h = min(meth.timestep(b) for b in twins)
+        for b in twins:
+            meth.fill_ghosts_periodic(b)
+            meth.compute(b, dt_h)
+        dt_o = min(O.timestep(prm, ob) for ob in obs)
+        for ob in obs:
+            O.fill_ghosts_periodic(ob)
+            O.step(prm, ob, dt_o)
+        torch.cuda.synchronize()
+        assert float(dmin[0]) == dt_h
+        if dtype == torch.float64:
+            assert dt_h == dt_o
+        for b, t, ob in zip(blks, twins, obs):
+            got, twin = b.to_numpy(), t.to_numpy()
+            for k in got:
+                assert np.array_equal(got[k], twin[k]), k
+                if dtype == torch.float64:
+                    assert np.array_equal(got[k], ob.f[ic.ORACLE_NAME[k]]), k
+                else:
+                    assert rel_l1(got[k].astype(np.float64), ob.f[ic.ORACLE_NAME[k]]) <= 2e-5, k

@@ -76,3 +76,37 @@ def test_fp64_boundary_fluxes_match_reference_golden(case):
     got = {f"{ax}{side}{q}": digest(t.cpu().numpy()) for (ax, side, q), t in sorted(fc.items())}
     assert got == rec["fc_sha256"]
     assert digest(blk.to_numpy()["density"]) == rec["output_sha256"]["density"]
+
+
+# ------------------------------------------------------------ edge cases
+from golden_edge_input import EDGE_CASES, N as EN, G as EG  # noqa: E402
+
+EDGE = json.load(open(os.path.join(HERE, "golden", "golden_edge.json")))
+EDGE_DENS = np.load(os.path.join(HERE, "golden", "golden_edge_density.npz"))
+
+
+def _run_edge(case, dtype):
+    name, solver, recon, de, eta, dfloor, pfloor, build = case
+    mhd = solver != "hllc"
+    state = build()
+    meth = B.EnzoMethodMHDVlct(
+        mhd_choice="constrained_transport" if mhd else "no_bfield",
+        riemann_solver=solver, reconstruct_method=recon, dual_energy=de,
+        dual_energy_eta=eta, density_floor=dfloor, pressure_floor=pfloor)
+    blk = B.Block(EN, EG, WIDTHS, mhd=mhd, dual_energy=de, dtype=dtype)
+    blk.load_numpy(state)
+    dt = meth.timestep(blk)
+    meth.compute(blk, dt)
+    torch.cuda.synchronize()
+    return dt, blk.to_numpy()
+
+
+@pytest.mark.parametrize("case", EDGE_CASES, ids=[c[0] for c in EDGE_CASES])
+def test_fp64_matches_reference_edge_golden_bit_exact(case):
+    """Degenerate HLLD states, active floors and the dual-energy switch at a
+    Mach-10 jump: the CUDA FP64 path reproduces the reference bit for bit."""
+    rec = EDGE["cases"][case[0]]
+    dt, out = _run_edge(case, torch.float64)
+    assert dt.hex() == rec["dt"]
+    got = {k: digest(out[k]) for k in rec["output_sha256"]}
+    assert got == rec["output_sha256"]

@@ -95,6 +95,39 @@ def test_noalloc_passive_scalars_match_allocating_step(solver, recon, de, scheme
     assert "passive_2" in a.to_numpy()
 
 
+@pytest.mark.parametrize("recon,dtype,npass,gravity", [
+    ("plm", torch.float64, 0, True),   # the gravity source on the full-dt stage
+    ("nn", torch.float32, 2, False),   # FP32 scalars in the two-CTA NN instantiation
+    ("plm", torch.float32, 1, True),
+])
+def test_noalloc_extras_match_allocating_step(recon, dtype, npass, gravity):
+    n = (10, 8, 9)
+    state, w = ic.smooth_block(n, 3, seed=29)
+    rng = np.random.default_rng(7)
+    shp = state["density"].shape
+    for k in range(npass):
+        state[f"passive_{k}"] = state["density"] * (0.2 + 0.6 * rng.random(shp))
+    if gravity:
+        for k in ("acceleration_x", "acceleration_y", "acceleration_z"):
+            state[k] = 0.3 * (rng.random(shp) - 0.5)
+    meth = B.EnzoMethodMHDVlct(riemann_solver="hlld", reconstruct_method=recon)
+    a, b = (B.Block(n, 3, w, dtype=dtype, npassive=npass, gravity=gravity) for _ in range(2))
+    a.load_numpy(state)
+    b.load_numpy(state)
+    for _ in range(2):
+        dt = meth.timestep(a)
+        assert meth.timestep(b) == dt
+        meth.fill_ghosts_periodic(a)
+        meth.fill_ghosts_periodic(b)
+        meth.compute(a, dt)
+        assert _noalloc_step(meth, b, dt) == capi.MHD_OK
+        torch.cuda.synchronize()
+        _same(a, b)
+    if npass:
+        assert not np.array_equal(a.to_numpy()["passive_0"],
+                                  np.asarray(state["passive_0"], dtype=a.to_numpy()["passive_0"].dtype))
+
+
 def test_noalloc_geometry_change_between_calls():
     # a larger block after a smaller one reuses the same static array
     for n in ((6, 6, 6), (16, 10, 12), (6, 6, 6)):
