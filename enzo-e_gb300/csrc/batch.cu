@@ -109,6 +109,13 @@ struct mhdvlct_batch {
   int threads[2] = {256, 256};  // CTA size of each stage's launches
   std::map<std::vector<int>, TileChoice> tune;  // per block-size class
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // stream-ordered batch (a serving request's): every device allocation and
+  // free is ordered on `ost` (cudaMallocAsync / cudaFreeAsync), and set-up
+  // copies run on it, so creating and destroying the batch never waits for
+  // work on other streams
+  bool ordered = false;
+  cudaStream_t ost = nullptr;
+  cudaMemPool_t mpool = nullptr;  // the pool of an ordered batch (null: default)
   std::string err;
 
   template <class R> R* ptr(size_t o) const { return (R*)pool + o; }
@@ -120,6 +127,24 @@ int bfail(mhdvlct_batch* b, int code, const std::string& m) {
   b->err = m;
   if (b->h) b->h->err = m;
   return code;
+}
+
+// Device memory of a batch: stream-ordered on the batch's stream for an
+// ordered batch, plain cudaMalloc / cudaFree otherwise.
+cudaError_t bmalloc(mhdvlct_batch* b, void** p, size_t n) {
+  if (!b->ordered) return cudaMalloc(p, n);
+  return b->mpool ? cudaMallocFromPoolAsync(p, n, b->mpool, b->ost)
+                  : cudaMallocAsync(p, n, b->ost);
+}
+void bfree(mhdvlct_batch* b, void* p) {
+  if (!p) return;
+  if (b->ordered) cudaFreeAsync(p, b->ost);
+  else cudaFree(p);
+}
+// The stream of a batch's own set-up work (its ordered stream, else the
+// caller's).
+cudaStream_t setup_stream(const mhdvlct_batch* b, cudaStream_t st) {
+  return b->ordered ? b->ost : st;
 }
 
 void drop_graphs(mhdvlct_batch* b) {
@@ -262,10 +287,11 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
     b->tile_tx[s] = tx[s];
     b->tile_ty[s] = ty[s];
   }
+  st = setup_stream(b, st);
   auto upload = [&](void** dst, const void* src, size_t bytes) -> int {
-    if (*dst) cudaFree(*dst);
+    if (*dst) bfree(b, *dst);
     *dst = nullptr;
-    if (cudaMalloc(dst, std::max<size_t>(bytes, 16)) != cudaSuccess)
+    if (bmalloc(b, dst, std::max<size_t>(bytes, 16)) != cudaSuccess)
       return bfail(b, MHD_ERR_NOMEM, "descriptor allocation");
     if (cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
       return bfail(b, MHD_ERR_CUDA, "descriptor upload");
@@ -407,6 +433,14 @@ extern "C" int mhdvlct_batch_create_ex(mhdvlct_handle* h, const int* dims,
                                        const double* widths, int nblocks, int ghost,
                                        int dtype, int npassive, int gravity,
                                        mhdvlct_batch** out) {
+  return mhdint::batch_create(h, dims, widths, nblocks, ghost, dtype, npassive, gravity,
+                              nullptr, nullptr, out);
+}
+
+int mhdint::batch_create(mhdvlct_handle* h, const int* dims, const double* widths,
+                         int nblocks, int ghost, int dtype, int npassive, int gravity,
+                         cudaStream_t ordered_stream, cudaMemPool_t pool,
+                         mhdvlct_batch** out) {
   if (!h || !dims || !widths || !out || nblocks <= 0) return MHD_ERR_INVALID;
   *out = nullptr;
   if (npassive < 0 || npassive > 4 || (gravity != 0 && gravity != 1))
@@ -418,6 +452,9 @@ extern "C" int mhdvlct_batch_create_ex(mhdvlct_handle* h, const int* dims,
     return fail(h, MHD_ERR_GHOST, "ghost depth must be at least 3");
   mhdvlct_batch* b = new mhdvlct_batch();
   b->h = h;
+  b->ordered = ordered_stream != nullptr;
+  b->ost = ordered_stream;
+  b->mpool = pool;
   b->dtype = dtype;
   b->nblocks = nblocks;
   b->g = ghost;
@@ -488,27 +525,38 @@ extern "C" int mhdvlct_batch_create_ex(mhdvlct_handle* h, const int* dims,
     }
   }
   b->pool_bytes = o * esz;
-  cudaError_t e = cudaMalloc(&b->pool, b->pool_bytes);
+  cudaError_t e = bmalloc(b, &b->pool, b->pool_bytes);
   if (e != cudaSuccess) {
+    b->pool = nullptr;
     delete b;
     return fail(h, MHD_ERR_NOMEM, std::string("batch pool: ") + cudaGetErrorString(e));
   }
-  cudaMemset(b->pool, 0, b->pool_bytes);
-  bool ok = cudaMalloc((void**)&b->d_queue, 2 * sizeof(int)) == cudaSuccess &&
-            cudaMalloc((void**)&b->d_nbr, 27 * sizeof(int) * (size_t)nblocks) == cudaSuccess &&
-            cudaMalloc((void**)&b->d_dt, sizeof(double) * (size_t)nblocks) == cudaSuccess &&
-            cudaMalloc((void**)&b->d_dtmin, sizeof(double)) == cudaSuccess &&
-            cudaMalloc((void**)&b->d_time, sizeof(double)) == cudaSuccess &&
-            cudaMalloc(&b->d_smax, 3 * sizeof(unsigned long long) * (size_t)nblocks) == cudaSuccess;
+  bool ok = bmalloc(b, (void**)&b->d_queue, 2 * sizeof(int)) == cudaSuccess &&
+            bmalloc(b, (void**)&b->d_nbr, 27 * sizeof(int) * (size_t)nblocks) == cudaSuccess &&
+            bmalloc(b, (void**)&b->d_dt, sizeof(double) * (size_t)nblocks) == cudaSuccess &&
+            bmalloc(b, (void**)&b->d_dtmin, sizeof(double)) == cudaSuccess &&
+            bmalloc(b, (void**)&b->d_time, sizeof(double)) == cudaSuccess &&
+            bmalloc(b, &b->d_smax, 3 * sizeof(unsigned long long) * (size_t)nblocks) ==
+                cudaSuccess;
   if (!ok) {
     mhdvlct_batch_destroy(b);
     return fail(h, MHD_ERR_NOMEM, "batch descriptors");
   }
-  cudaMemset(b->d_time, 0, sizeof(double));
   std::vector<int> nbr(27 * (size_t)nblocks);
   for (int i = 0; i < nblocks; i++)
     for (int k = 0; k < 27; k++) nbr[27 * (size_t)i + k] = i;
-  cudaMemcpy(b->d_nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (b->ordered) {
+    // everything on the batch's own stream; build_descriptors below waits
+    // for that stream (and only it) before the host vector goes away
+    cudaMemsetAsync(b->pool, 0, b->pool_bytes, b->ost);
+    cudaMemsetAsync(b->d_time, 0, sizeof(double), b->ost);
+    cudaMemcpyAsync(b->d_nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice,
+                    b->ost);
+  } else {
+    cudaMemset(b->pool, 0, b->pool_bytes);
+    cudaMemset(b->d_time, 0, sizeof(double));
+    cudaMemcpy(b->d_nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice);
+  }
   b->grid = 0;
   if (int rc = build_descriptors_any(b, 0)) {
     mhdvlct_batch_destroy(b);
@@ -520,30 +568,33 @@ extern "C" int mhdvlct_batch_create_ex(mhdvlct_handle* h, const int* dims,
 
 extern "C" int mhdvlct_batch_destroy(mhdvlct_batch* b) {
   if (!b) return MHD_ERR_INVALID;
-  cudaDeviceSynchronize();
+  // an ordered batch frees on its own stream after the work queued there;
+  // any other batch waits for the device (its memory may be in use on any
+  // stream the caller ran it on)
+  if (!b->ordered) cudaDeviceSynchronize();
   drop_graphs(b);
   for (int p = 0; p < 2; p++) {
-    for (int s = 0; s < 2; s++) cudaFree(b->d_sblocks[p][s]);
-    cudaFree(b->d_aux[p]);
+    for (int s = 0; s < 2; s++) bfree(b, b->d_sblocks[p][s]);
+    bfree(b, b->d_aux[p]);
   }
-  for (int s = 0; s < 2; s++) cudaFree(b->d_tiles[s]);
-  cudaFree(b->d_queue);
-  cudaFree(b->d_nbr);
-  if (b->d_rf) cudaFree(b->d_rf);
-  cudaFree(b->d_flux);
-  cudaFree(b->d_fluxout);
-  cudaFree(b->d_fcplan);
-  cudaFree(b->d_gtiles);
-  cudaFree(b->d_gqueue);
+  for (int s = 0; s < 2; s++) bfree(b, b->d_tiles[s]);
+  bfree(b, b->d_queue);
+  bfree(b, b->d_nbr);
+  bfree(b, b->d_rf);
+  bfree(b, b->d_flux);
+  bfree(b, b->d_fluxout);
+  bfree(b, b->d_fcplan);
+  bfree(b, b->d_gtiles);
+  bfree(b, b->d_gqueue);
   for (cudaEvent_t x : b->ev) cudaEventDestroy(x);
   if (b->s_d2h) cudaStreamDestroy(b->s_d2h);
   if (b->s_h2d) cudaStreamDestroy(b->s_h2d);
-  cudaFree(b->d_dt);
-  cudaFree(b->d_dtmin);
-  cudaFree(b->d_time);
-  cudaFree(b->d_smax);
-  cudaFree(b->d_diag);
-  cudaFree(b->pool);
+  bfree(b, b->d_dt);
+  bfree(b, b->d_dtmin);
+  bfree(b, b->d_time);
+  bfree(b, b->d_smax);
+  bfree(b, b->d_diag);
+  bfree(b, b->pool);
   delete b;
   return MHD_OK;
 }
@@ -567,7 +618,7 @@ int set_flux_correction_t(mhdvlct_batch* b, unsigned quantities, const MhdRefres
   int nq = 0;
   for (int q = 0; q < 6; q++) nq += (quantities >> q) & 1u;
   const size_t per_block = 2 * (face_elems[0] + face_elems[1] + face_elems[2]) * nq;
-  if (cudaMalloc(&b->d_flux, per_block * b->nblocks * sizeof(R)) != cudaSuccess) {
+  if (bmalloc(b, &b->d_flux, per_block * b->nblocks * sizeof(R)) != cudaSuccess) {
     b->d_flux = nullptr;
     return bfail(b, MHD_ERR_NOMEM, "flux buffers");
   }
@@ -592,8 +643,8 @@ int set_flux_correction_t(mhdvlct_batch* b, unsigned quantities, const MhdRefres
   int rc = plan_flux_correct(b->h, views.data(), b->nblocks, fcs.data(), faces, nfaces,
                              conservative, b->fcplan);
   if (rc != MHD_OK) return bfail(b, rc, b->h->err);
-  if (cudaMalloc(&b->d_fluxout, outs.size() * sizeof(FluxOut<R>)) != cudaSuccess ||
-      cudaMalloc((void**)&b->d_fcplan, std::max<size_t>(b->fcplan.blob.size(), 16)) !=
+  if (bmalloc(b, &b->d_fluxout, outs.size() * sizeof(FluxOut<R>)) != cudaSuccess ||
+      bmalloc(b, (void**)&b->d_fcplan, std::max<size_t>(b->fcplan.blob.size(), 16)) !=
           cudaSuccess)
     return bfail(b, MHD_ERR_NOMEM, "flux-correction tables");
   cudaError_t e = cudaMemcpy(b->d_fluxout, outs.data(), outs.size() * sizeof(FluxOut<R>),
@@ -614,9 +665,9 @@ extern "C" int mhdvlct_batch_set_flux_correction(mhdvlct_batch* b, unsigned quan
     return MHD_ERR_INVALID;
   cudaDeviceSynchronize();
   b->fc_on = false;
-  cudaFree(b->d_flux);
-  cudaFree(b->d_fluxout);
-  cudaFree(b->d_fcplan);
+  bfree(b, b->d_flux);
+  bfree(b, b->d_fluxout);
+  bfree(b, b->d_fcplan);
   b->d_flux = b->d_fluxout = nullptr;
   b->d_fcplan = nullptr;
   b->fcplan = FluxCorrectPlan();
@@ -642,7 +693,7 @@ extern "C" int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefres
                                                int nfaces, unsigned conservative) {
   if (!b || nfaces < 0 || (nfaces > 0 && !faces)) return MHD_ERR_INVALID;
   drop_graphs(b);
-  if (b->d_rf) cudaFree(b->d_rf);
+  bfree(b, b->d_rf);
   b->d_rf = nullptr;
   b->rf_nchunks = -1;
   if (nfaces == 0) return MHD_OK;  // back to the 27-neighbour refresh
@@ -666,7 +717,7 @@ extern "C" int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefres
   memcpy(host.data() + b->rf_ptr[1], plan[1].ptrs.data(), bp);
   memcpy(host.data() + b->rf_items, plan[0].items.data(), plan[0].items.size());
   memcpy(host.data() + b->rf_chunks, plan[0].chunks.data(), plan[0].chunks.size());
-  if (cudaMalloc((void**)&b->d_rf, total) != cudaSuccess) {
+  if (bmalloc(b, (void**)&b->d_rf, total) != cudaSuccess) {
     b->d_rf = nullptr;
     return bfail(b, MHD_ERR_NOMEM, "refresh tables");
   }
@@ -874,13 +925,13 @@ int setup_host_groups(mhdvlct_batch* b, int ngroups) {
       if (group_of[t.block] == g) sorted.push_back(t);
     b->hg_ntile[g] = (int)sorted.size() - b->hg_tile0[g];
   }
-  cudaFree(b->d_gtiles);
-  cudaFree(b->d_gqueue);
+  bfree(b, b->d_gtiles);
+  bfree(b, b->d_gqueue);
   b->d_gtiles = nullptr;
   b->d_gqueue = nullptr;
-  if (cudaMalloc((void**)&b->d_gtiles, std::max<size_t>(1, sorted.size()) * sizeof(StageTile)) !=
+  if (bmalloc(b, (void**)&b->d_gtiles, std::max<size_t>(1, sorted.size()) * sizeof(StageTile)) !=
           cudaSuccess ||
-      cudaMalloc((void**)&b->d_gqueue, ng * sizeof(int)) != cudaSuccess)
+      bmalloc(b, (void**)&b->d_gqueue, ng * sizeof(int)) != cudaSuccess)
     return bfail(b, MHD_ERR_NOMEM, "host-run tables");
   cudaError_t e = cudaMemcpy(b->d_gtiles, sorted.data(), sorted.size() * sizeof(StageTile),
                              cudaMemcpyHostToDevice);
@@ -1045,6 +1096,8 @@ extern "C" int mhdvlct_batch_state_segments(mhdvlct_batch* b, void** dev_ptrs,
   return MHD_OK;
 }
 
+const double* mhdint::batch_time_device(const mhdvlct_batch* b) { return b->d_time; }
+
 extern "C" int mhdvlct_batch_state_region(mhdvlct_batch* b, void** dev_ptr,
                                           size_t* bytes) {
   if (!b || !dev_ptr || !bytes) return MHD_ERR_INVALID;
@@ -1093,14 +1146,14 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
   // save the state so the trial steps leave no trace
   const size_t bytes = b->state_elems * sizeof(R);
   void* save = nullptr;
-  if (cudaMalloc(&save, bytes) != cudaSuccess)
+  if (bmalloc(b, &save, bytes) != cudaSuccess)
     return bfail(b, MHD_ERR_NOMEM, "autotune state copy");
   const int parity0 = b->parity;
   cudaMemcpyAsync(save, b->pool, bytes, cudaMemcpyDeviceToDevice, st);
   // a dt for the trial steps (per-block CFL of the current state)
   cudaError_t e = launch_timestep_b<R>(b, 0, st);
   if (e != cudaSuccess) {
-    cudaFree(save);
+    bfree(b, save);
     return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
   }
   const int tmax = TileLimits<R>::TMAX;
@@ -1182,7 +1235,7 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
           ncand++;
           b->tune[cls] = c;
           if (int rc = build_descriptors<R>(b, st)) {
-            cudaFree(save);
+            bfree(b, save);
             return rc;
           }
           // one untimed step, then reps timed steps
@@ -1232,7 +1285,7 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
   b->parity = parity0;
   cudaMemcpyAsync(b->pool, save, bytes, cudaMemcpyDeviceToDevice, st);
   cudaStreamSynchronize(st);
-  cudaFree(save);
+  bfree(b, save);
   if (e != cudaSuccess) return bfail(b, MHD_ERR_CUDA, cudaGetErrorString(e));
   return build_descriptors<R>(b, st);
 }
@@ -1256,9 +1309,9 @@ extern "C" int mhdvlct_batch_diagnostics(mhdvlct_batch* b, double* out, void* st
   const int rows = b->nblocks * cpb;
   if (!b->d_diag || b->diag_rows < rows) {
     cudaStreamSynchronize(st);
-    cudaFree(b->d_diag);
+    bfree(b, b->d_diag);
     b->d_diag = nullptr;
-    if (cudaMalloc((void**)&b->d_diag, ((size_t)rows + 1) * NDIAG * sizeof(double)) !=
+    if (bmalloc(b, (void**)&b->d_diag, ((size_t)rows + 1) * NDIAG * sizeof(double)) !=
         cudaSuccess) {
       b->d_diag = nullptr;
       return bfail(b, MHD_ERR_NOMEM, "diagnostics scratch");

@@ -62,6 +62,18 @@ vlct::FieldSet<R> fieldset_of(const MhdBlockView* b);
 // Default tile extent for a precision (fits the shared-memory budget).
 int default_tile(int dtype, int solver, int recon, int de, int np = 0);
 
+// The batched form (batch.cu).  batch_create is mhdvlct_batch_create_ex with,
+// when ordered_stream is not null, every device allocation, free and set-up
+// copy of the batch ordered on that stream (cudaMallocFromPoolAsync from
+// `pool`, or cudaMallocAsync when pool is null; cudaFreeAsync), so that
+// creating or destroying it never waits for other streams' work.
+int batch_create(mhdvlct_handle* h, const int* dims, const double* widths, int nblocks,
+                 int ghost, int dtype, int npassive, int gravity,
+                 cudaStream_t ordered_stream, cudaMemPool_t pool, mhdvlct_batch** out);
+// Device address of the batch's simulated-time accumulator: the sum of dt
+// over the cycles of the last mhdvlct_batch_run call.
+const double* batch_time_device(const mhdvlct_batch* b);
+
 // Mesh ghost refresh (refresh.cu): a validated plan of refresh faces over a
 // set of block views -- the per-block field pointer table and the device
 // records of the regions and their CTA chunks.

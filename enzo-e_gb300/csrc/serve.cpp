@@ -3,24 +3,30 @@
 // Each request is a periodic box of n^3 cells advanced `cycles` VL+CT cycles
 // in FP32 with its own Riemann solver / reconstruction.  Requests queue on
 // submit; the scheduler admits them (first fit, in arrival order) whenever
-// the device-memory budget and the active-slot limit allow, uploads their
-// state once, and enqueues all their cycles on a private stream, so the work
-// of every active request overlaps on the device.  Completion is detected by
-// polling an event; the final state is copied to a host buffer, the request's
-// device memory is released and waiting requests are admitted into the freed
-// room.  Each request's dt comes from its own CFL reduction in a private
-// device slot, so a result does not depend on what else is running.
+// the device-memory budget and the active-slot limit allow.  Admission
+// enqueues the whole request on a private stream: the upload of its initial
+// state from a pinned staging buffer, the ghost refresh, every cycle, and the
+// download of its final state back into the same staging buffer, so the work
+// of every active request overlaps on the device and the host never waits
+// for it.  The request's device memory comes from the server's stream-ordered
+// memory pool and is freed in stream order too, so neither admission nor
+// retirement waits for other requests' work (a cudaMalloc / cudaFree or a
+// device synchronisation would).  Completion is detected by polling an
+// event; the host then copies the active cells out of the staging buffer.
+// Each request's dt comes from its own CFL reduction in a private device
+// slot, so a result does not depend on what else is running.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <deque>
 #include <string>
 #include <vector>
 
-#include "../../include/mhdvlct_gb300.h"
+#include "capi_internal.h"
 
 namespace {
 
@@ -30,6 +36,13 @@ double now_s() {
 }
 
 enum { Q_QUEUED = 0, Q_RUNNING = 1, Q_DONE = 2, Q_FAILED = 3 };
+
+// A pinned host staging buffer, reused by later requests once free.
+struct Pinned {
+  char* p = nullptr;
+  size_t bytes = 0;
+  bool busy = false;
+};
 
 struct Req {
   int ticket = 0;
@@ -42,6 +55,8 @@ struct Req {
   mhdvlct_batch* b = nullptr;
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
+  int pin = -1;  // staging buffer (index into the server's list)
+  void* d_out = nullptr;  // the packed final state and its non-finite count
   size_t bytes = 0;
   double t_submit = 0, t_admit = 0, t_done = 0, sim_time = 0;
   std::vector<float> result[8];
@@ -57,6 +72,38 @@ size_t request_bytes(int n, int g, int mhd, int de) {
   return 4 * (2 * cells * M + (mhd ? 9 * F : 0) + M) + (1 << 20);
 }
 
+// Staging layout of a request: the uploaded fields back to back (cells of
+// m^3, faces of (m+1) m^2, 256-byte aligned), reused for the downloaded cell
+// fields, and the simulated time in the last 8 bytes.
+size_t stage_offset(int k, size_t M, size_t F) {
+  size_t o = 0;
+  for (int j = 0; j < k; j++) o += ((j < 8 ? M : F) * sizeof(float) + 255) & ~(size_t)255;
+  return o;
+}
+size_t stage_bytes(int nf, size_t M, size_t F) { return stage_offset(nf, M, F) + 256; }
+
+// The active cells of the final cell fields packed densely (field after
+// field, x fastest) and the number of non-finite values among them, so that
+// completion is one contiguous copy and no host pass over the state.
+struct PackSrc {
+  const float* f[8];
+};
+__global__ void pack_active_kernel(PackSrc src, int nf, int n, int g, float* out,
+                                   unsigned* bad) {
+  const size_t m = (size_t)n + 2 * g, nn = (size_t)n * n, cells = nn * n;
+  unsigned local = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < cells * nf;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i / cells);
+    const size_t c = i - (size_t)k * cells;
+    const size_t z = c / nn, y = (c / n) % n, x = c % n;
+    const float v = src.f[k][((z + g) * m + (y + g)) * m + (x + g)];
+    out[i] = v;
+    local += isfinite(v) ? 0u : 1u;
+  }
+  if (local) atomicAdd(bad, local);
+}
+
 }  // namespace
 
 struct mhdserve {
@@ -67,6 +114,8 @@ struct mhdserve {
   std::vector<Req*> reqs;
   std::deque<int> queue;
   std::vector<int> active;
+  std::vector<Pinned> pinned;
+  cudaMemPool_t pool = nullptr;  // device memory of every request
   std::string err;
 };
 
@@ -78,14 +127,19 @@ int sfail(mhdserve* s, int code, const std::string& m) {
 }
 
 void release(mhdserve* s, Req* r) {
+  // the batch frees its memory on the request's stream, after its work
+  if (r->d_out) cudaFreeAsync(r->d_out, r->st);
+  r->d_out = nullptr;
   if (r->b) mhdvlct_batch_destroy(r->b);
   if (r->h) mhdvlct_destroy(r->h);
   if (r->done) cudaEventDestroy(r->done);
-  if (r->st) cudaStreamDestroy(r->st);
+  if (r->st) cudaStreamDestroy(r->st);  // returns at once; the frees still run
   r->b = nullptr;
   r->h = nullptr;
   r->done = nullptr;
   r->st = nullptr;
+  if (r->pin >= 0) s->pinned[r->pin].busy = false;
+  r->pin = -1;
   s->in_use -= std::min(s->in_use, r->bytes);
   for (auto& v : r->init) std::vector<float>().swap(v);
 }
@@ -94,51 +148,110 @@ void fail_req(mhdserve* s, Req* r, const std::string& m) {
   r->err = m;
   r->state = Q_FAILED;
   r->t_done = now_s();
+  // a request that fails after its work was queued must not hand its staging
+  // buffer on before that work is over
+  if (r->st) cudaStreamSynchronize(r->st);
   release(s, r);
 }
 
-// Admit one request: allocate, upload, refresh ghosts, enqueue every cycle.
+// A free staging buffer of at least `bytes` (the smallest that fits), or a
+// new one; -1 if pinned memory cannot be had.
+int take_pinned(mhdserve* s, size_t bytes) {
+  int best = -1;
+  for (int i = 0; i < (int)s->pinned.size(); i++) {
+    const Pinned& p = s->pinned[i];
+    if (!p.busy && p.bytes >= bytes && (best < 0 || p.bytes < s->pinned[best].bytes)) best = i;
+  }
+  if (best < 0) {
+    Pinned p;
+    if (cudaHostAlloc((void**)&p.p, bytes, cudaHostAllocDefault) != cudaSuccess) return -1;
+    p.bytes = bytes;
+    s->pinned.push_back(p);
+    best = (int)s->pinned.size() - 1;
+  }
+  s->pinned[best].busy = true;
+  return best;
+}
+
+// Admit one request: allocate, then enqueue upload, refresh, every cycle and
+// the download of the final state on the request's stream.
 bool start(mhdserve* s, Req* r) {
   int rc = mhdvlct_create(&r->params, &r->h);
   if (rc != MHD_OK) {
     fail_req(s, r, std::string("create: ") + (r->h ? mhdvlct_last_error_string(r->h) : ""));
     return false;
   }
-  const int dims[3] = {r->n, r->n, r->n};
-  const double w = r->box / r->n;
-  const double widths[3] = {w, w, w};
   s->in_use += r->bytes;
-  rc = mhdvlct_batch_create(r->h, dims, widths, 1, 3, MHD_DTYPE_F32, &r->b);
-  if (rc != MHD_OK) {
-    fail_req(s, r, std::string("batch: ") + mhdvlct_last_error_string(r->h));
-    return false;
-  }
   if (cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming) != cudaSuccess) {
     fail_req(s, r, "stream/event creation");
     return false;
   }
+  const int dims[3] = {r->n, r->n, r->n};
+  const double w = r->box / r->n;
+  const double widths[3] = {w, w, w};
+  rc = mhdint::batch_create(r->h, dims, widths, 1, 3, MHD_DTYPE_F32, 0, 0, r->st, s->pool,
+                            &r->b);
+  if (rc != MHD_OK) {
+    fail_req(s, r, std::string("batch: ") + mhdvlct_last_error_string(r->h));
+    return false;
+  }
+  const int g = 3;
+  const size_t m = (size_t)r->n + 2 * g;
+  const size_t M = m * m * m, F = (m + 1) * m * m;
+  const int nf = r->mhd ? 11 : 5;
+  r->pin = take_pinned(s, stage_bytes(nf, M, F));
+  if (r->pin < 0) {
+    fail_req(s, r, "pinned staging buffer");
+    return false;
+  }
+  char* stage = s->pinned[r->pin].p;
   MhdBlockView v;
   mhdvlct_batch_block_view(r->b, 0, &v);
-  void* dst[12] = {v.density, v.velocity[0], v.velocity[1], v.velocity[2],
+  void* dst[11] = {v.density, v.velocity[0], v.velocity[1], v.velocity[2],
                    v.total_energy, v.bfield[0], v.bfield[1], v.bfield[2],
-                   v.bfieldi[0], v.bfieldi[1], v.bfieldi[2], nullptr};
-  const int nf = r->mhd ? 11 : 5;
+                   v.bfieldi[0], v.bfieldi[1], v.bfieldi[2]};
   for (int k = 0; k < nf; k++) {
-    if (r->init[k].empty()) continue;
-    if (cudaMemcpyAsync(dst[k], r->init[k].data(), r->init[k].size() * sizeof(float),
+    char* h = stage + stage_offset(k, M, F);
+    std::memcpy(h, r->init[k].data(), r->init[k].size() * sizeof(float));
+    if (cudaMemcpyAsync(dst[k], h, r->init[k].size() * sizeof(float),
                         cudaMemcpyHostToDevice, r->st) != cudaSuccess) {
       fail_req(s, r, "upload");
       return false;
     }
   }
-  // the host copy must stay alive until the copies have run
-  cudaStreamSynchronize(r->st);
   for (auto& x : r->init) std::vector<float>().swap(x);
   if (mhdvlct_batch_refresh(r->b, r->st) != MHD_OK ||
-      mhdvlct_batch_run(r->b, r->cycles, 1, nullptr, r->st) != MHD_OK ||
-      cudaEventRecord(r->done, r->st) != cudaSuccess) {
+      mhdvlct_batch_run(r->b, r->cycles, 1, nullptr, r->st) != MHD_OK) {
     fail_req(s, r, std::string("launch: ") + mhdvlct_last_error_string(r->h));
+    return false;
+  }
+  // the final cell fields (the same arrays whatever the face-buffer parity)
+  // packed on the device with their non-finite count, then one copy of that
+  // and one of the simulated time into the staging buffer
+  const int nd = r->mhd ? 8 : 5;
+  const size_t active = (size_t)r->n * r->n * r->n;
+  const size_t out_bytes = nd * active * sizeof(float);
+  PackSrc ps{};
+  const void* src[8] = {v.density, v.velocity[0], v.velocity[1], v.velocity[2],
+                        v.total_energy, v.bfield[0], v.bfield[1], v.bfield[2]};
+  for (int k = 0; k < nd; k++) ps.f[k] = (const float*)src[k];
+  bool ok = cudaMallocFromPoolAsync(&r->d_out, out_bytes + 256, s->pool, r->st) == cudaSuccess;
+  unsigned* d_bad = ok ? (unsigned*)((char*)r->d_out + out_bytes) : nullptr;
+  if (ok) ok = cudaMemsetAsync(d_bad, 0, sizeof(unsigned), r->st) == cudaSuccess;
+  if (ok) {
+    const int grid = (int)std::min<size_t>((nd * active + 255) / 256, 4096);
+    pack_active_kernel<<<grid, 256, 0, r->st>>>(ps, nd, r->n, g, (float*)r->d_out, d_bad);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  if (ok)
+    ok = cudaMemcpyAsync(stage, r->d_out, out_bytes + sizeof(unsigned), cudaMemcpyDeviceToHost,
+                         r->st) == cudaSuccess &&
+         cudaMemcpyAsync(stage + stage_offset(nf, M, F), mhdint::batch_time_device(r->b),
+                         sizeof(double), cudaMemcpyDeviceToHost, r->st) == cudaSuccess &&
+         cudaEventRecord(r->done, r->st) == cudaSuccess;
+  if (!ok) {
+    fail_req(s, r, "download");
     return false;
   }
   r->state = Q_RUNNING;
@@ -146,37 +259,26 @@ bool start(mhdserve* s, Req* r) {
   return true;
 }
 
+// A request whose event has completed: its packed final state, the count of
+// non-finite values in it and its simulated time are in the staging buffer.
 void finish(mhdserve* s, Req* r) {
-  MhdBlockView v;
-  mhdvlct_batch_block_view(r->b, 0, &v);
-  double t = 0;
-  mhdvlct_batch_run(r->b, 0, 1, &t, r->st);
-  r->sim_time = t;
-  const int g = 3, n = r->n, m = n + 2 * g;
-  void* src[8] = {v.density, v.velocity[0], v.velocity[1], v.velocity[2],
-                  v.total_energy, v.bfield[0], v.bfield[1], v.bfield[2]};
-  const int nf = r->mhd ? 8 : 5;
-  std::vector<float> full((size_t)m * m * m);
-  bool finite = true;
-  for (int k = 0; k < nf; k++) {
-    if (cudaMemcpy(full.data(), src[k], full.size() * sizeof(float),
-                   cudaMemcpyDeviceToHost) != cudaSuccess) {
-      fail_req(s, r, "download");
-      return;
-    }
-    r->result[k].resize((size_t)n * n * n);
-    for (int z = 0; z < n; z++)
-      for (int y = 0; y < n; y++)
-        for (int x = 0; x < n; x++) {
-          const float val = full[((size_t)(z + g) * m + (y + g)) * m + (x + g)];
-          finite = finite && std::isfinite(val);
-          r->result[k][((size_t)z * n + y) * n + x] = val;
-        }
-  }
+  const int g = 3, n = r->n;
+  const size_t m = (size_t)n + 2 * g;
+  const size_t M = m * m * m, F = (m + 1) * m * m;
+  const int nf = r->mhd ? 11 : 5, nd = r->mhd ? 8 : 5;
+  const size_t active = (size_t)n * n * n;
+  const char* stage = s->pinned[r->pin].p;
+  std::memcpy(&r->sim_time, stage + stage_offset(nf, M, F), sizeof(double));
+  unsigned bad = 0;
+  std::memcpy(&bad, stage + nd * active * sizeof(float), sizeof(unsigned));
   r->t_done = now_s();
-  if (!finite) {
+  if (bad) {
     fail_req(s, r, "non-finite state");
     return;
+  }
+  for (int k = 0; k < nd; k++) {
+    const float* f = (const float*)stage + k * active;
+    r->result[k].assign(f, f + active);
   }
   r->state = Q_DONE;
   release(s, r);
@@ -191,6 +293,28 @@ extern "C" int mhdserve_create(const MhdVlctParams* base, size_t budget,
   s->base = *base;
   s->budget = budget;
   s->max_active = max_active;
+  // the requests' device memory: a pool of the current device that keeps
+  // what the finished requests freed (up to the budget) for the next ones
+  int dev = 0;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      (props.location.id = dev, cudaMemPoolCreate(&s->pool, &props)) != cudaSuccess) {
+    delete s;
+    return MHD_ERR_CUDA;
+  }
+  uint64_t keep = budget;
+  cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  // reserve the budget now: one allocation of it, freed back into the pool,
+  // so that admissions never wait for the pool to map new memory
+  void* p = nullptr;
+  if (cudaMallocFromPoolAsync(&p, budget, s->pool, 0) == cudaSuccess) {
+    cudaFreeAsync(p, 0);
+    cudaStreamSynchronize(0);
+  } else {
+    cudaGetLastError();  // a budget beyond free memory: the pool grows on demand
+  }
   *out = s;
   return MHD_OK;
 }
@@ -202,6 +326,10 @@ extern "C" int mhdserve_destroy(mhdserve* s) {
     release(s, r);
     delete r;
   }
+  // every request's stream-ordered frees must have run before the pool goes
+  cudaDeviceSynchronize();
+  if (s->pool) cudaMemPoolDestroy(s->pool);
+  for (Pinned& p : s->pinned) cudaFreeHost(p.p);
   delete s;
   return MHD_OK;
 }
