@@ -67,3 +67,38 @@ def test_ghost_fill_periodic_copies_interior():
     fx = b.f["bfx"]
     assert np.array_equal(fx[:, :, 0:3], fx[:, :, 6:9])
     assert np.array_equal(fx[:, :, 10:13], fx[:, :, 4:7])
+
+
+# The slow wave and the HLLC sound wave at N=16 (input/vlct/
+# run_MHD_linear_wave_test.py:184, run_HD_linear_wave_test.py:70); the N=32
+# norms run on the CUDA path in tests/test_gpu_known_answers.py.
+@pytest.mark.parametrize("wave,stop,ref,mhd,solver", [
+    ("slow", 2.0, 2.2373810027584788e-07, True, O.HLLD),
+    ("sound", 1.0, 1.3704437791196907e-07, False, O.HLLC),
+])
+def test_linear_wave_golden_l1_slow_and_sound(wave, stop, ref, mhd, solver):
+    l1 = _linear_wave(wave, 16, stop, mhd, solver)
+    assert abs(l1 - ref) / ref < 1e-8, (l1, ref)
+
+
+def test_passive_sound_wave_golden_l1():
+    """input/vlct/run_passive_advect_sound_test.py:66, x-aligned: the L1
+    norm over the hydro fields, B and the passive scalar after one period."""
+    import known_answers as K
+    state, n, w = K.passive_sound(0)
+    b = O.Block(n, 3, w, mhd=True, npassive=1)
+    for k, v in state.items():
+        if k == "red":
+            b.f["pass0"][...] = v
+        elif ic.ORACLE_NAME.get(k) in b.f:
+            b.f[ic.ORACLE_NAME[k]][...] = v
+    prm = O.params(riemann=O.HLLD, recon=O.PLM, mhd=True, theta_limiter=2.0,
+                   gamma=G53, courant=0.4)
+    O.evolve_periodic(prm, b, 1.0)
+    got = {k: b.f[ic.ORACLE_NAME[k]] for k in state if k in ic.ORACLE_NAME}
+    got["red"] = b.f["pass0"]
+    names = ["density", "velocity_x", "velocity_y", "velocity_z", "total_energy",
+             "bfield_x", "bfield_y", "bfield_z", "red"]
+    l1 = K.sim_l1(state, got, names, 3, n)
+    ref = 6.918011605252798e-08
+    assert abs(l1 - ref) / ref < 1e-8, (l1, ref)
