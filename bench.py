@@ -286,6 +286,41 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _compute_roofline(zone_rate, stage_ms, zones):
+    """The compute side of the roofline (the kernels are issue-bound, not
+    HBM-bound): the instruction issue of the dominant stage kernel against the
+    GPU's issue rate, and the FP32 operations of the cycle against the FP32
+    peak, from the per-zone figures of the committed ncu summary
+    (profiles/ncu_instructions.json) and of the op-counting oracle
+    (profiles/flops_per_zone.json).  Peaks are nominal: 152 SMs x 4 schedulers
+    x 1 warp-instruction per cycle, and 152 SMs x 128 FP32 lanes x 2 (FMA),
+    at the maximum SM clock."""
+    try:
+        ins = json.load(open(os.path.join(ROOT, "profiles", "ncu_instructions.json")))["per_zone"]
+        alg = json.load(open(os.path.join(ROOT, "profiles", "flops_per_zone.json")))
+        alg_flops = alg["configs"]["hlld_plm"]["flops_per_zone_update"]
+    except (OSError, KeyError, ValueError):
+        return None
+    nsm, clk = 152, 2.07e9
+    issue_peak = nsm * 4 * clk
+    fp32_peak = nsm * 128 * 2 * clk / 1e12
+    s2 = ins["stage2_full_dt"]
+    issue = s2["warp_inst"] * zones / (stage_ms["stage2_full_dt"] / 1e3)
+    flops_exec = ins["stage1_half_dt"]["fp32_flops"] + s2["fp32_flops"]
+    return {
+        "bound": "issue", "kernel": "stage2_full_dt", "unit": "warp-inst/s",
+        "achieved": issue, "peak": issue_peak, "frac": issue / issue_peak,
+        "peak_kind": "nominal (152 SMs x 4 schedulers x 1 warp-inst/cycle x 2070 MHz)",
+        "warp_inst_per_zone": s2["warp_inst"],
+        "fp32": {"flops_per_zone_algorithmic": alg_flops,
+                 "flops_per_zone_executed": flops_exec,
+                 "achieved_tflops": flops_exec * zone_rate / 1e12,
+                 "peak_tflops": fp32_peak, "frac": flops_exec * zone_rate / 1e12 / fp32_peak,
+                 "arithmetic_intensity_flop_per_byte": alg_flops / (5 * N_STATE * 4),
+                 "ridge_flop_per_byte": fp32_peak * 1e12 / (_peaks()[0] * 1e9),
+                 "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2070 MHz)"}}
+
+
 def _traffic(kernel_key, zones):
     """DRAM bytes per launch of the dominant kernel: the ncu-measured bytes
     per active zone of that kernel (profiles/ncu_traffic.json, captured on a
@@ -1237,7 +1272,9 @@ def main():
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": dom_bytes,
-                         "cycle_frac": value / world * 5 * N_STATE * 4 / 1e9 / peak},
+                         "cycle_frac": value / world * 5 * N_STATE * 4 / 1e9 / peak,
+                         "compute": _compute_roofline(value / world, {"stage2_full_dt": k_s2},
+                                                      zones)},
             "kernels_ms_per_step": {"timestep": k_ts, "refresh": k_ref,
                                     "stage1_half_dt": k_s1, "stage2_full_dt": k_s2,
                                     "cycle": k_cyc},

@@ -172,8 +172,12 @@ int mhdvlct_block_step_device_dt(mhdvlct_handle* h, const MhdBlockView* b,
                                  const double* dt_dev, void* stream);
 
 /* No counterpart in the reference (the reference's compute allocates its
- * scratch through EnzoVlctScratchSpace on the host heap).  Same operation and
- * results as mhdvlct_block_step, but allocates no device memory: its scratch
+ * scratch through EnzoVlctScratchSpace on the host heap).  For callers that
+ * cannot call cudaMalloc: a host whose device memory is all claimed up front
+ * by its own allocator (a pool sized at start-up), or one that must not make
+ * a call that may synchronise the whole device while other streams run.
+ * Same operation and results as mhdvlct_block_step, but allocates no device
+ * memory: its scratch
  * is one file-scope __device__ array of 8 MiB (8388608 bytes) per device,
  * whose address is taken with cudaGetSymbolAddress on the first call on each
  * device and cached.  Make that first call on a device outside stream
