@@ -255,65 +255,76 @@ refresh_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ n
   }
 }
 
-// The same refresh with the per-field set-up hoisted out of the element loop:
-// one thread fills shared memory with the 27 source arrays of the field and
-// the multiply-high constants of the shell decode, so an element costs a few
-// integer multiplies, one shared load, one global load and one store.  Exact
-// while every numerator times divisor stays below 2^32, which the host checks
-// (blocks up to ~150^3 cells with 3 ghost layers); larger blocks use
+// The same refresh, cell-major: a thread decodes one ghost-shell position
+// once and copies every cell-centred field of the block there (the fields'
+// source arrays for all 27 neighbour offsets staged in shared memory once
+// per CTA), then the face-centred fields follow over their own shells.  The
+// copies are the same as refresh_kernel's element for element (every source
+// is an active cell of its block, so the order of the copies is free).  The
+// shell decode divides by a multiply-high with ceil(2^32 / d), exact while
+// every numerator times divisor stays below 2^32, which the host checks
+// (blocks up to ~250 cells per side with 3 ghost layers); larger blocks use
 // refresh_kernel.
 template <class R>
 __global__ void __launch_bounds__(256)
-refresh_fast_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ nbr,
-                    int nblocks, int g, int nfield_slots, int chunks_per_block) {
-  __shared__ R* s_src[27];
-  __shared__ R* s_dst;
-  __shared__ unsigned s_magic[5];
+refresh_shell_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restrict__ nbr,
+                     int nblocks, int g, int chunks_per_block) {
+  // cell-centred slots: the 9 cell fields, the pressure field, 4 passive
+  // scalars, 3 acceleration components
+  constexpr int NC = NCELL + 8;
+  __shared__ R* s_src[NC][27];
+  __shared__ R* s_dst[NC];
+  __shared__ R* s_fsrc[3][27];
+  __shared__ R* s_fdst[3];
+  __shared__ int s_slot[NC];
+  __shared__ int s_nc;
   const int b = blockIdx.x / chunks_per_block;
   const int chunk = blockIdx.x - b * chunks_per_block;
   if (b >= nblocks) return;
   const AuxBlock<R>& B = blocks[b];
+  auto cell_slot = [](const AuxBlock<R>& X, int fs) -> R* {
+    if (fs < NCELL) return X.f.c[fs];
+    if (fs == NCELL) return X.pressure;
+    if (fs < NCELL + 5) return X.pass[fs - NCELL - 1];
+    return X.accel[fs - NCELL - 5];
+  };
+  if (threadIdx.x == 0) {
+    int k = 0;
+    for (int fs = 0; fs < NC; fs++)
+      if (cell_slot(B, fs)) s_slot[k++] = fs;
+    s_nc = k;
+  }
+  __syncthreads();
+  const int nc = s_nc;
+  for (int i = threadIdx.x; i < nc * 27; i += blockDim.x) {
+    const int j = i / 27, k = i - 27 * j;
+    s_src[j][k] = cell_slot(blocks[nbr[27 * b + k]], s_slot[j]);
+  }
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) s_dst[j] = cell_slot(B, s_slot[j]);
+  for (int i = threadIdx.x; i < 81; i += blockDim.x) {
+    const int d = i / 27, k = i - 27 * d;
+    s_fsrc[d][k] = B.f.f[d] ? blocks[nbr[27 * b + k]].f.f[d] : nullptr;
+    if (k == 0) s_fdst[d] = B.f.f[d];
+  }
+  __syncthreads();
   const int n[3] = {B.m[0] - 2 * g, B.m[1] - 2 * g, B.m[2] - 2 * g};
   auto magic = [](unsigned d) -> unsigned { return d > 1 ? 0xFFFFFFFFu / d + 1u : 0u; };
   auto mdiv = [](int v, unsigned d, unsigned m) -> int {
     return d > 1 ? (int)__umulhi((unsigned)v, m) : v;
   };
-  for (int fs = 0; fs < nfield_slots; fs++) {
-    auto slot_ptr = [&](const AuxBlock<R>& X) -> R* {
-      if (fs < NCELL) return X.f.c[fs];
-      if (fs < NCELL + 3) return X.f.f[fs - NCELL];
-      if (fs == NCELL + 3) return X.pressure;
-      if (fs < NCELL + 8) return X.pass[fs - NCELL - 4];
-      return X.accel[fs - NCELL - 8];
-    };
-    // a field this block does not hold: skip it before the barriers (the
-    // test is uniform over the CTA)
-    if (!slot_ptr(B)) continue;
-    const int face = (fs >= NCELL && fs < NCELL + 3) ? fs - NCELL : -1;
-    int e[3], lo[3], hi[3];
+  // face = -1: the cell-centred shell (all cell fields); 0..2: the shell of
+  // bfieldi along that axis
+  for (int face = -1; face < 3; face++) {
+    if (face >= 0 && !s_fdst[face]) continue;
+    int e[3], hi[3];
     for (int a = 0; a < 3; a++) {
       e[a] = B.m[a] + (a == face);
-      lo[a] = g;
       hi[a] = (a == face) ? g + n[a] + 1 : g + n[a];
     }
-    const int wz = e[2] - (hi[2] - lo[2]), wy = e[1] - (hi[1] - lo[1]),
-              wx = e[0] - (hi[0] - lo[0]);
-    const int iz = hi[2] - lo[2], iy = hi[1] - lo[1];
-    __syncthreads();  // the previous field's readers are done
-    if (threadIdx.x < 27) s_src[threadIdx.x] = slot_ptr(blocks[nbr[27 * b + threadIdx.x]]);
-    if (threadIdx.x == 32) {
-      s_dst = slot_ptr(B);
-      s_magic[0] = magic(e[0]);
-      s_magic[1] = magic(e[1]);
-      s_magic[2] = magic(wy);
-      s_magic[3] = magic(wx);
-      s_magic[4] = magic(iy);
-    }
-    __syncthreads();
-    R* dst = s_dst;
-    if (!dst) continue;
-    const unsigned m0 = s_magic[0], m1 = s_magic[1], mwy = s_magic[2], mwx = s_magic[3],
-                   miy = s_magic[4];
+    const int wz = e[2] - (hi[2] - g), wy = e[1] - (hi[1] - g), wx = e[0] - (hi[0] - g);
+    const int iz = hi[2] - g, iy = hi[1] - g;
+    const unsigned m0 = magic(e[0]), m1 = magic(e[1]), mwy = magic(wy), mwx = magic(wx),
+                   miy = magic(iy);
     const int cz = wz * e[1] * e[0];
     const int cy = iz * wy * e[0];
     const int cx = iz * iy * wx;
@@ -326,23 +337,23 @@ refresh_fast_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restric
         x = q - r1 * e[0];
         const int r2 = mdiv(r1, e[1], m1);
         y = r1 - r2 * e[1];
-        z = (r2 < lo[2]) ? r2 : r2 + iz;
+        z = (r2 < g) ? r2 : r2 + iz;
       } else if (q < cz + cy) {
         const int r0 = q - cz;
         const int r1 = mdiv(r0, e[0], m0);
         x = r0 - r1 * e[0];
         const int r2 = mdiv(r1, wy, mwy);
         const int yy = r1 - r2 * wy;
-        y = (yy < lo[1]) ? yy : yy + iy;
-        z = lo[2] + r2;
+        y = (yy < g) ? yy : yy + iy;
+        z = g + r2;
       } else {
         const int r0 = q - cz - cy;
         const int r1 = mdiv(r0, wx, mwx);
         const int xx = r0 - r1 * wx;
-        x = (xx < lo[0]) ? xx : xx + (hi[0] - lo[0]);
+        x = (xx < g) ? xx : xx + (hi[0] - g);
         const int r2 = mdiv(r1, iy, miy);
-        y = lo[1] + (r1 - r2 * iy);
-        z = lo[2] + r2;
+        y = g + (r1 - r2 * iy);
+        z = g + r2;
       }
       // source index and neighbour offset per axis; a face axis keeps the
       // block's own boundary faces (k = g, g + n)
@@ -351,12 +362,18 @@ refresh_fast_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restric
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         const int i = idx[a];
-        const int top = (a == face) ? g + n[a] + 1 : g + n[a];
-        side[a] = (i < g) ? -1 : ((i >= top) ? 1 : 0);
+        side[a] = (i < g) ? -1 : ((i >= hi[a]) ? 1 : 0);
         src[a] = i - side[a] * n[a];
       }
-      const R* sp = s_src[(side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1)];
-      dst[((size_t)z * e[1] + y) * e[0] + x] = sp[((size_t)src[2] * e[1] + src[1]) * e[0] + src[0]];
+      const int k = (side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1);
+      const size_t di = ((size_t)z * e[1] + y) * e[0] + x;
+      const size_t si = ((size_t)src[2] * e[1] + src[1]) * e[0] + src[0];
+      if (face < 0) {
+#pragma unroll 4
+        for (int j = 0; j < nc; j++) s_dst[j][di] = s_src[j][k][si];
+      } else {
+        s_fdst[face][di] = s_fsrc[face][k][si];
+      }
     }
   }
 }

@@ -133,11 +133,11 @@ cudaError_t launch_timestep<VLCT_REAL>(bool mhd, bool de,
 template <>
 cudaError_t launch_refresh<VLCT_REAL>(const AuxBlock<VLCT_REAL>* b, const int* nbr,
                                       int nb, int g, int cpb, int max_m, cudaStream_t st) {
-  // the decode of refresh_fast_kernel is exact while (shell elements of a
+  // the decode of refresh_shell_kernel is exact while (shell elements of a
   // field) x (largest divisor) < 2^32; bound the shell by the whole field
   const unsigned long long mm = (unsigned long long)max_m + 1;
   if (mm * mm * mm * mm < (1ull << 32))
-    refresh_fast_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 11, cpb);
+    refresh_shell_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, cpb);
   else
     refresh_kernel<VLCT_REAL><<<nb * cpb, 256, 0, st>>>(b, nbr, nb, g, NCELL + 11, cpb);
   return cudaGetLastError();

@@ -77,6 +77,21 @@ __device__ __forceinline__ R limiter_enzo_rk(R vm1, R v, R vp1, R theta) {
   R sr = (R(0.0) < dv_r) ? R(1.0) : ((dv_r < R(0.0)) ? R(-1.0) : R(0.0));
   return (R(0.5) * (sl + sr)) * min3(fabs(dv_l), fabs(dv_r), fabs(dv_c));
 }
+// The same limiter in FP32 with fewer instructions: 0.5 (sgn dl + sgn dr) is
+// +-1 when the two one-sided differences share a sign and 0 otherwise (a zero
+// difference makes the minimum zero), so the slope is the minimum magnitude
+// carrying dl's sign when dl dr > 0, else 0 -- the same value, as sign times
+// minimum is exact either way (a product dl dr below the FP32 range flushes
+// to 0 under -ftz, as do such differences themselves).
+template <>
+__device__ __forceinline__ float limiter_enzo_rk<float>(float vm1, float v, float vp1,
+                                                        float theta) {
+  const float dv_c = 0.5f * (vp1 - vm1);
+  const float dv_l = (v - vm1) * theta;
+  const float dv_r = (vp1 - v) * theta;
+  const float m = fminf(fminf(fabsf(dv_l), fabsf(dv_r)), fabsf(dv_c));
+  return (dv_l * dv_r > 0.f) ? copysignf(m, dv_l) : 0.f;
+}
 // PLM_AthenaLimiter (EnzoReconstructorPLM.hpp:337-345)
 template <class R>
 __device__ __forceinline__ R limiter_athena(R vm1, R v, R vp1) {
