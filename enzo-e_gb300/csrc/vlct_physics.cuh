@@ -316,6 +316,125 @@ __device__ __forceinline__ void hlld(R g, const R* wli, const R* wri,
   }
 }
 
+// HLLD in FP32: the same states and flux with shared denominators taken
+// once (one reciprocal per denominator, rsqrt for 1/sqrt(rho*)), and the
+// flux selected by its jump coefficients instead of forming every jump.
+template <>
+__device__ __forceinline__ void hlld<float>(float g, const float* wli, const float* wri,
+                                            FaceFlux<float>& out) {
+  const float SMALL = 1.0e-8f;
+  const float igm1 = 1.0f / (g - 1.0f);
+  const float pl = wli[L_E], pr = wri[L_E];
+  const float bxi = wli[L_BI], bxsq = bxi * bxi;
+  const float dl = wli[L_RHO], dr = wri[L_RHO];
+  const float ul = wli[L_VI], ur = wri[L_VI];
+  const float inv_dl = 1.0f / dl, inv_dr = 1.0f / dr;
+  const float btl = wli[L_BJ] * wli[L_BJ] + wli[L_BK] * wli[L_BK];
+  const float btr = wri[L_BJ] * wri[L_BJ] + wri[L_BK] * wri[L_BK];
+  const float pbl = 0.5f * (bxsq + btl), pbr = 0.5f * (bxsq + btr);
+  const float kel = 0.5f * dl * (ul * ul + (wli[L_VJ] * wli[L_VJ] + wli[L_VK] * wli[L_VK]));
+  const float ker = 0.5f * dr * (ur * ur + (wri[L_VJ] * wri[L_VJ] + wri[L_VK] * wri[L_VK]));
+  const float ule = pl * igm1 + kel + pbl, ure = pr * igm1 + ker + pbr;
+  // fast speeds (EnzoEOSIdeal.hpp:133-139)
+  auto cf = [&](float p, float inv_d, float bt) {
+    const float c2 = g * p * inv_d, va2 = (bxsq + bt) * inv_d, vac2 = bxsq * inv_d;
+    const float q = c2 + va2;
+    return sqrtf(0.5f * (va2 + c2 + sqrtf(q * q - 4.f * c2 * vac2)));
+  };
+  const float cfl = cf(pl, inv_dl, btl), cfr = cf(pr, inv_dr, btr);
+  const float spd0 = fminf(ul - cfl, ur - cfr);
+  const float spd4 = fmaxf(ul + cfl, ur + cfr);
+  const float ptl = pl + pbl, ptr = pr + pbr;
+  // left / right fluxes: d, mx, my, mz, e, by, bz
+  const float ulby = wli[L_BJ], ulbz = wli[L_BK], urby = wri[L_BJ], urbz = wri[L_BK];
+  const float FL[7] = {dl * ul, dl * ul * ul + ptl - bxsq, dl * wli[L_VJ] * ul - bxi * ulby,
+                       dl * wli[L_VK] * ul - bxi * ulbz,
+                       ul * (ule + ptl - bxsq) - bxi * (wli[L_VJ] * ulby + wli[L_VK] * ulbz),
+                       ulby * ul - bxi * wli[L_VJ], ulbz * ul - bxi * wli[L_VK]};
+  const float FR[7] = {dr * ur, dr * ur * ur + ptr - bxsq, dr * wri[L_VJ] * ur - bxi * urby,
+                       dr * wri[L_VK] * ur - bxi * urbz,
+                       ur * (ure + ptr - bxsq) - bxi * (wri[L_VJ] * urby + wri[L_VK] * urbz),
+                       urby * ur - bxi * wri[L_VJ], urbz * ur - bxi * wri[L_VK]};
+  const float sdl = spd0 - ul, sdr = spd4 - ur;
+  const float spd2 = (sdr * dr * ur - sdl * dl * ul + (ptl - ptr)) / (sdr * dr - sdl * dl);
+  const float sdml = spd0 - spd2, sdmr = spd4 - spd2;
+  const float lst_d = dl * sdl / sdml, rst_d = dr * sdr / sdmr;
+  const float isql = rsqrtf(lst_d), isqr = rsqrtf(rst_d);
+  const float sqrtdl = lst_d * isql, sqrtdr = rst_d * isqr;
+  const float lst_d_inv = isql * isql, rst_d_inv = isqr * isqr;
+  const float spd1 = spd2 - fabsf(bxi) * isql;
+  const float spd3 = spd2 + fabsf(bxi) * isqr;
+  const float ptst = 0.5f * ((ptr + dr * sdr * (spd2 - ur)) + (ptl + dl * sdl * (spd2 - ul)));
+  // single-star states: d, mx, my, mz, e, by, bz
+  float Ls[7], Rs[7];
+  auto star = [&](const float* w, float d, float sd, float sdm, float st_d, float st_d_inv,
+                  float by, float bz, float ue, float pt, float* S) {
+    S[0] = st_d;
+    S[1] = st_d * spd2;
+    const float den = d * sd * sdm - bxsq;
+    if (fabsf(den) < SMALL * ptst) {
+      S[2] = st_d * w[L_VJ]; S[3] = st_d * w[L_VK]; S[5] = by; S[6] = bz;
+    } else {
+      const float iden = 1.0f / den;
+      const float t1 = bxi * (sd - sdm) * iden;
+      S[2] = st_d * (w[L_VJ] - by * t1);
+      S[3] = st_d * (w[L_VK] - bz * t1);
+      const float t2 = (d * (sd * sd) - bxsq) * iden;
+      S[5] = by * t2; S[6] = bz * t2;
+    }
+    const float vbst = (S[1] * bxi + (S[2] * S[5] + S[3] * S[6])) * st_d_inv;
+    S[4] = (sd * ue - pt * w[L_VI] + ptst * spd2 +
+            bxi * (w[L_VI] * bxi + (w[L_VJ] * by + w[L_VK] * bz) - vbst)) / sdm;
+    return vbst;
+  };
+  const float vbstl = star(wli, dl, sdl, sdml, lst_d, lst_d_inv, ulby, ulbz, ule, ptl, Ls);
+  const float vbstr = star(wri, dr, sdr, sdmr, rst_d, rst_d_inv, urby, urbz, ure, ptr, Rs);
+  // double-star states
+  float Ld[7], Rd[7];
+#pragma unroll
+  for (int k = 0; k < 7; k++) { Ld[k] = Ls[k]; Rd[k] = Rs[k]; }
+  if (!(0.5f * bxsq < SMALL * ptst)) {
+    const float invsumd = 1.0f / (sqrtdl + sqrtdr);
+    const float bxsig = bxi > 0.0f ? 1.0f : -1.0f;
+    const float vyl = Ls[2] * lst_d_inv, vyr = Rs[2] * rst_d_inv;
+    const float vzl = Ls[3] * lst_d_inv, vzr = Rs[3] * rst_d_inv;
+    const float ty = invsumd * (sqrtdl * vyl + sqrtdr * vyr + bxsig * (Rs[5] - Ls[5]));
+    const float tz = invsumd * (sqrtdl * vzl + sqrtdr * vzr + bxsig * (Rs[6] - Ls[6]));
+    Ld[2] = Ls[0] * ty; Rd[2] = Rs[0] * ty;
+    Ld[3] = Ls[0] * tz; Rd[3] = Rs[0] * tz;
+    const float sq = bxsig * sqrtdl * sqrtdr;
+    const float by = invsumd * (sqrtdl * Rs[5] + sqrtdr * Ls[5] + sq * (vyr - vyl));
+    const float bz = invsumd * (sqrtdl * Rs[6] + sqrtdr * Ls[6] + sq * (vzr - vzl));
+    Ld[5] = Rd[5] = by; Ld[6] = Rd[6] = bz;
+    const float t = spd2 * bxi + (Ld[2] * by + Ld[3] * bz) * lst_d_inv;
+    Ld[4] = Ls[4] - sqrtdl * bxsig * (vbstl - t);
+    Rd[4] = Rs[4] + sqrtdr * bxsig * (vbstr - t);
+  }
+  // F = F_side + c1 (U* - U) + c2 (U** - U*), the cases in the reference's
+  // order: F_L (spd0 >= 0), F_R (spd4 <= 0), then by the signs of spd1..spd3
+  const bool outer = spd0 >= 0.0f || spd4 <= 0.0f;
+  const bool left = spd0 >= 0.0f || (!(spd4 <= 0.0f) && spd2 >= 0.0f);
+  const float c1 = outer ? 0.0f : (left ? spd0 : spd4);
+  const float c2 = outer ? 0.0f : (left ? (spd1 >= 0.0f ? 0.0f : spd1)
+                                        : (spd3 > 0.0f ? spd3 : 0.0f));
+  const float U0[7] = {dl, dl * ul, dl * wli[L_VJ], dl * wli[L_VK], ule, ulby, ulbz};
+  const float U1[7] = {dr, dr * ur, dr * wri[L_VJ], dr * wri[L_VK], ure, urby, urbz};
+  float Fo[7];
+#pragma unroll
+  for (int k = 0; k < 7; k++) {
+    const float F = left ? FL[k] : FR[k], U = left ? U0[k] : U1[k];
+    const float Us = left ? Ls[k] : Rs[k], Ud = left ? Ld[k] : Rd[k];
+    Fo[k] = F + c1 * (Us - U) + c2 * (Ud - Us);
+  }
+  out.f[L_RHO] = Fo[0]; out.f[L_VI] = Fo[1]; out.f[L_VJ] = Fo[2]; out.f[L_VK] = Fo[3];
+  out.f[L_E] = Fo[4]; out.f[L_BJ] = Fo[5]; out.f[L_BK] = Fo[6];
+  out.f[L_BI] = 0.0f;
+  out.eflux = eint_flux(g, dl, pl, dr, pr, out.f[L_RHO]);
+  if (spd0 > 0.0f) out.vbar = ul;
+  else if (spd4 < 0.0f) out.vbar = ur;
+  else out.vbar = spd2 * (spd2 >= 0.0f ? sdl / sdml : sdr / sdmr);
+}
+
 // conserved state from primitives (EnzoRiemannUtils.hpp:48-82)
 template <class R, bool MHD>
 __device__ __forceinline__ void conserved(R g, const R* w, R* u) {

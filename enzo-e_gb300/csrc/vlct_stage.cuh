@@ -6,17 +6,18 @@
 // state read and the stage's outputs stays in shared memory: the primitives
 // and cell-centred E of a ring of z-planes, the x/y face fluxes of two
 // planes, the z-face fluxes of two faces, the edge EMFs and the new face B.
-// Per z-plane t the CTA runs four phases separated by __syncthreads():
+// Per z-plane t the CTA runs three phases separated by __syncthreads():
 //
 //   B  Riemann solves: z-faces at t+1/2, x- and y-faces of plane t+1 (when
 //      the boundary fluxes are stored, a short pass after B copies the
 //      tile's block-boundary faces out of shared memory)
 //   C  upwinded edge EMFs: E_x, E_y at t+1/2 and E_z of plane t
-//   D1 constrained-transport face updates (Bz at t+1/2, Bx / By of plane t),
-//      and the primitives + cell-centred E of plane t+1+L (L = 1 for NN, 2
-//      for PLM) loaded into the ring for the next plane
-//   D2 cell updates of plane t: centred B, flux divergence + dual-energy
-//      source, density floor, energy floor / dual-energy sync; store.
+//   D  per column of the tile: its constrained-transport face updates (Bz
+//      at t+1, Bx / By at both faces of cell t), then the cell update of
+//      plane t -- centred B, flux divergence + dual-energy source, density
+//      floor, energy floor / dual-energy sync, store -- and the primitives
+//      + cell-centred E of plane t+1+L (L = 1 for NN, 2 for PLM) loaded into
+//      the ring for the next plane.
 //
 // The index windows of every quantity are those of the reference's array
 // passes (EnzoMHDIntegratorStageCommands::compute_update_stage,
@@ -82,7 +83,7 @@ struct SmemLayout {
   int PP, QP;   // primitive tile pitch / rows
   int HP, HQ;   // halo grid pitch / rows (tile + 1 cell each side)
   int G;        // HP * HQ
-  int o_prim, o_xf, o_yf, o_zf, o_ec, o_ex, o_ey, o_ez, o_bx, o_by, o_bz;
+  int o_prim, o_xf, o_yf, o_zf, o_ec, o_ex, o_ey, o_ez, o_bz;
   int o_pprim, o_pf;  // passive scalars: specific-form ring, face fluxes
   int total;    // in elements of R
   __host__ __device__ void init(int tx, int ty, int rp, int nring, int nf, int np = 0) {
@@ -100,8 +101,6 @@ struct SmemLayout {
     o_ex = o; o += 2 * G;
     o_ey = o; o += 2 * G;
     o_ez = o; o += G;
-    o_bx = o; o += G;
-    o_by = o; o += G;
     o_bz = o; o += 2 * G;
     o_pprim = o; o += nring * np * PP * QP;
     o_pf = o; o += 3 * 2 * np * G;  // [dir][slot][scalar]
@@ -176,8 +175,6 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   R* s_ex = sm + Ls.o_ex;
   R* s_ey = sm + Ls.o_ey;
   R* s_ez = sm + Ls.o_ez;
-  R* s_bx = sm + Ls.o_bx;
-  R* s_by = sm + Ls.o_by;
   R* s_bz = sm + Ls.o_bz;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int s = info.s, S = info.S;
@@ -562,77 +559,48 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         }
         __syncthreads();
       }
-      // ---- D1: face updates (EnzoBfieldMethodCT.cpp:617-687); a face that
-      // is not updated in this stage keeps its start-of-step value.  The
-      // primitives of plane t+1+LOOK (next step) load in the same phase.
-      if (MHD) {
+      // ---- D: per column (x, y) of the tile, the constrained-transport
+      // face updates it needs (EnzoBfieldMethodCT.cpp:617-687) -- Bz at the
+      // face t+1 above it and, when plane t is output, Bx at faces x, x+1 and
+      // By at faces y, y+1 of plane t -- then the update of cell (x, y, t).
+      // A face between two cells of the tile is computed by both (the same
+      // expression) and written by the one that owns it: the cell on its high
+      // side, or the cell below the block's outermost written face.  A face
+      // not updated in this stage keeps its start-of-step value.  Bz at t+1
+      // stays in shared memory for the same column's next plane, so the
+      // mapping of columns to threads is the same for every plane.  The
+      // primitives of plane t+1+LOOK load into the ring in the same phase.
+      {
         const bool do_plane = t >= za;
         // the lowest face of a chunk is written by the chunk below it
         const bool own_bz = t >= za || za == olo;
-        for (int idx = tid; idx < 3 * G; idx += nthr) {
-          const int kind = idx < G ? 0 : (idx < 2 * G ? 1 : 2), r = idx - kind * G;
-          const int j = divHP.div(r), i = r - j * HP;
-          const int x = hx0 + i, y = hy0 + j;
-          if (kind == 0) {  // Bz at face kz = t+1 of column (x, y)
-            if (i < 1 || i > tx || j < 1 || j > ty) continue;
-            const int kz = t + 1;
-            if (kz > m2) continue;
-            const size_t fi = (size_t)kz * cstr_z + (size_t)y * cstr_y + x;
-            const bool upd = inr(kz, S + 1, m2 - S) && inr(x, S + 1, m0 - S - 1) &&
-                             inr(y, S + 1, m1 - S - 1);
-            R v;
-            if (upd) {
-              const R Ek_term = dtdx[0] * (s_ey[(t & 1) * G + r] - s_ey[(t & 1) * G + r - 1]);
-              const R Ej_term = dtdx[1] * (s_ex[(t & 1) * G + r] - s_ex[(t & 1) * G + r - HP]);
-              v = B.base.f[2][fi] - Ek_term + Ej_term;
-              if (own_bz) B.out.f[2][fi] = v;
-            } else {
-              v = B.base.f[2][fi];
-            }
-            s_bz[(kz & 1) * G + r] = v;
-          } else if (kind == 1) {  // Bx at face kx = x of plane t
-            if (!do_plane || i < 1 || i > tx + 1 || j < 1 || j > ty) continue;
-            const int kx = x;
-            const size_t fi = (size_t)t * ((size_t)m1 * (m0 + 1)) + (size_t)y * (m0 + 1) + kx;
-            const bool upd = inr(kx, S + 1, m0 - S) && inr(y, S + 1, m1 - S - 1) &&
-                             inr(t, S + 1, m2 - S - 1);
-            R v;
-            if (upd) {
-              // E_z at (kx-1/2, y -+ 1/2), E_y at (kx-1/2, t -+ 1/2)
-              const int re = r - 1;  // edge ex = kx - 1
-              const R Ek_term = dtdx[1] * (s_ez[re] - s_ez[re - HP]);
-              const R Ej_term = dtdx[2] * (s_ey[(t & 1) * G + re] - s_ey[((t - 1) & 1) * G + re]);
-              v = B.base.f[0][fi] - Ek_term + Ej_term;
-              if (kx < xb || (kx == xb && xb == ohi_x)) B.out.f[0][fi] = v;
-            } else {
-              v = B.base.f[0][fi];
-            }
-            s_bx[r] = v;
-          } else {  // By at face ky = y of plane t
-            if (!do_plane || i < 1 || i > tx || j < 1 || j > ty + 1) continue;
-            const int ky = y;
-            const size_t fi = (size_t)t * ((size_t)(m1 + 1) * m0) + (size_t)ky * m0 + x;
-            const bool upd = inr(ky, S + 1, m1 - S) && inr(x, S + 1, m0 - S - 1) &&
-                             inr(t, S + 1, m2 - S - 1);
-            R v;
-            if (upd) {
-              // E_x at (x, ky-1/2, t -+ 1/2), E_z at (x -+ 1/2, ky-1/2)
-              const int re = r - HP;  // edge ey = ky - 1
-              const R Ek_term = dtdx[2] * (s_ex[(t & 1) * G + re] - s_ex[((t - 1) & 1) * G + re]);
-              const R Ej_term = dtdx[0] * (s_ez[re] - s_ez[re - 1]);
-              v = B.base.f[1][fi] - Ek_term + Ej_term;
-              if (ky < yb || (ky == yb && yb == ohi_y)) B.out.f[1][fi] = v;
-            } else {
-              v = B.base.f[1][fi];
-            }
-            s_by[r] = v;
-          }
-        }
-      }
-      if (t + 1 < zb) load_plane(t + 1 + LOOK);
-      __syncthreads();
-      // ---- D2: cell updates of plane t
-      if (t >= za) {
+        const bool in_t = inr(t, S + 1, m2 - S - 1);
+        // Bx at face kx of row y, plane t; rx: the halo index of face kx
+        auto face_x = [&](int kx, int y, int rx, bool own) -> R {
+          const size_t fi = (size_t)t * ((size_t)m1 * (m0 + 1)) + (size_t)y * (m0 + 1) + kx;
+          if (!(inr(kx, S + 1, m0 - S) && inr(y, S + 1, m1 - S - 1) && in_t))
+            return B.base.f[0][fi];
+          // E_z at (kx-1/2, y -+ 1/2), E_y at (kx-1/2, t -+ 1/2)
+          const int re = rx - 1;  // edge ex = kx - 1
+          const R Ek_term = dtdx[1] * (s_ez[re] - s_ez[re - HP]);
+          const R Ej_term = dtdx[2] * (s_ey[(t & 1) * G + re] - s_ey[((t - 1) & 1) * G + re]);
+          const R v = B.base.f[0][fi] - Ek_term + Ej_term;
+          if (own) B.out.f[0][fi] = v;
+          return v;
+        };
+        // By at face ky of column x, plane t; ry: the halo index of face ky
+        auto face_y = [&](int ky, int x, int ry, bool own) -> R {
+          const size_t fi = (size_t)t * ((size_t)(m1 + 1) * m0) + (size_t)ky * m0 + x;
+          if (!(inr(ky, S + 1, m1 - S) && inr(x, S + 1, m0 - S - 1) && in_t))
+            return B.base.f[1][fi];
+          // E_x at (x, ky-1/2, t -+ 1/2), E_z at (x -+ 1/2, ky-1/2)
+          const int re = ry - HP;  // edge ey = ky - 1
+          const R Ek_term = dtdx[2] * (s_ex[(t & 1) * G + re] - s_ex[((t - 1) & 1) * G + re]);
+          const R Ej_term = dtdx[0] * (s_ez[re] - s_ez[re - 1]);
+          const R v = B.base.f[1][fi] - Ek_term + Ej_term;
+          if (own) B.out.f[1][fi] = v;
+          return v;
+        };
         const R* xf0 = s_xf + (size_t)(t & 1) * NF * G;
         const R* yf0 = s_yf + (size_t)(t & 1) * NF * G;
         const R* zfm = s_zf + (size_t)((t - 1) & 1) * NF * G;
@@ -643,14 +611,40 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           const int qy = divT.div(idx);
           const int x = xa + (idx - qy * tx), y = ya + qy;
           const int r = (y - hy0) * HP + (x - hx0);
-          const size_t c = (size_t)t * cstr_z + (size_t)y * cstr_y + x;
-          const bool in_out = x < ohi_x && y < ohi_y;
-          if (!in_out) continue;
           R bcx = R(0), bcy = R(0), bcz = R(0);
-          if (MHD) {  // compute_center_bfield (EnzoBfieldMethodCT.cpp:702-728)
-            bcx = R(0.5) * (s_bx[r] + s_bx[r + 1]);
-            bcy = R(0.5) * (s_by[r] + s_by[r + HP]);
-            bcz = R(0.5) * (s_bz[(t & 1) * G + r] + s_bz[((t + 1) & 1) * G + r]);
+          if (MHD) {
+            // Bz at face kz = t+1 of column (x, y)
+            const int kz = t + 1;
+            R bz_hi = R(0);
+            if (kz <= m2) {
+              const size_t fi = (size_t)kz * cstr_z + (size_t)y * cstr_y + x;
+              const bool upd = inr(kz, S + 1, m2 - S) && inr(x, S + 1, m0 - S - 1) &&
+                               inr(y, S + 1, m1 - S - 1);
+              if (upd) {
+                const R Ek_term = dtdx[0] * (s_ey[(t & 1) * G + r] - s_ey[(t & 1) * G + r - 1]);
+                const R Ej_term = dtdx[1] * (s_ex[(t & 1) * G + r] - s_ex[(t & 1) * G + r - HP]);
+                bz_hi = B.base.f[2][fi] - Ek_term + Ej_term;
+                if (own_bz) B.out.f[2][fi] = bz_hi;
+              } else {
+                bz_hi = B.base.f[2][fi];
+              }
+            }
+            const R bz_lo = s_bz[(t & 1) * G + r];  // face t, from the previous plane
+            s_bz[((t + 1) & 1) * G + r] = bz_hi;
+            if (do_plane) {
+              // compute_center_bfield (EnzoBfieldMethodCT.cpp:702-728)
+              const R bx_lo = face_x(x, y, r, true);
+              const R bx_hi = face_x(x + 1, y, r + 1, x + 1 == xb && xb == ohi_x);
+              const R by_lo = face_y(y, x, r, true);
+              const R by_hi = face_y(y + 1, x, r + HP, y + 1 == yb && yb == ohi_y);
+              bcx = R(0.5) * (bx_lo + bx_hi);
+              bcy = R(0.5) * (by_lo + by_hi);
+              bcz = R(0.5) * (bz_lo + bz_hi);
+            }
+          }
+          if (!do_plane) continue;
+          const size_t c = (size_t)t * cstr_z + (size_t)y * cstr_y + x;
+          if (MHD) {
             B.out.c[F_BX][c] = bcx;
             B.out.c[F_BY][c] = bcy;
             B.out.c[F_BZ][c] = bcz;
@@ -728,6 +722,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           }
         }
       }
+      if (t + 1 < zb) load_plane(t + 1 + LOOK);
       __syncthreads();
     }
     // next tile: dynamic queue (persistent grid) or static grid stride
