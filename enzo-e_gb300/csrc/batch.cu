@@ -616,7 +616,7 @@ int set_flux_correction_t(mhdvlct_batch* b, unsigned quantities, const MhdRefres
   const int nx = b->dims[0], ny = b->dims[1], nz = b->dims[2];
   const size_t face_elems[3] = {(size_t)ny * nz, (size_t)nx * nz, (size_t)nx * ny};
   int nq = 0;
-  for (int q = 0; q < 6; q++) nq += (quantities >> q) & 1u;
+  for (int q = 0; q < MHD_FC_NQ; q++) nq += (quantities >> q) & 1u;
   const size_t per_block = 2 * (face_elems[0] + face_elems[1] + face_elems[2]) * nq;
   if (bmalloc(b, &b->d_flux, per_block * b->nblocks * sizeof(R)) != cudaSuccess) {
     b->d_flux = nullptr;
@@ -632,7 +632,7 @@ int set_flux_correction_t(mhdvlct_batch* b, unsigned quantities, const MhdRefres
     outs[i].g = b->g;
     for (int a = 0; a < 3; a++)
       for (int sd = 0; sd < 2; sd++)
-        for (int q = 0; q < 6; q++)
+        for (int q = 0; q < MHD_FC_NQ; q++)
           if ((quantities >> q) & 1u) {
             outs[i].f[a][sd][q] = p;
             fcs[i].flux[a][sd][q] = p;
@@ -661,7 +661,7 @@ int set_flux_correction_t(mhdvlct_batch* b, unsigned quantities, const MhdRefres
 extern "C" int mhdvlct_batch_set_flux_correction(mhdvlct_batch* b, unsigned quantities,
                                                  const MhdRefreshFace* faces, int nfaces,
                                                  unsigned conservative) {
-  if (!b || quantities >= (1u << 6) || nfaces < 0 || (nfaces > 0 && !faces))
+  if (!b || quantities >= (1u << MHD_FC_NQ) || nfaces < 0 || (nfaces > 0 && !faces))
     return MHD_ERR_INVALID;
   cudaDeviceSynchronize();
   b->fc_on = false;
@@ -677,6 +677,8 @@ extern "C" int mhdvlct_batch_set_flux_correction(mhdvlct_batch* b, unsigned quan
                    "Flux corrections are currently only supported in hydro-mode");
     if (((quantities >> MHD_Q_INTERNAL_ENERGY) & 1u) && !b->h->de)
       return bfail(b, MHD_ERR_INVALID, "internal_energy fluxes need dual energy");
+    if (quantities >> (MHD_Q_PASSIVE_0 + b->npass))
+      return bfail(b, MHD_ERR_INVALID, "a passive-scalar flux names a scalar the batch lacks");
     for (int i = 1; i < b->nblocks; i++)
       for (int a = 0; a < 3; a++)
         if (b->dims[3 * i + a] != b->dims[a])

@@ -17,6 +17,8 @@
 
 using namespace vlct;
 
+static_assert(kFluxQuantities == MHD_FC_NQ, "flux-correction quantity slots");
+
 namespace mhdint {
 
 int fail(mhdvlct_handle* h, int code, const std::string& msg) {
@@ -719,7 +721,7 @@ int block_step_on(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
     FluxOut<R> fo;
     for (int d = 0; d < 3; d++)
       for (int sd = 0; sd < 2; sd++)
-        for (int q = 0; q < 6; q++) fo.f[d][sd][q] = (R*)fc->flux[d][sd][q];
+        for (int q = 0; q < kFluxQuantities; q++) fo.f[d][sd][q] = (R*)fc->flux[d][sd][q];
     fo.g = b->ghost[0];
     e = put_bytes(S.d_fc, &fo, sizeof(fo), st);
     if (e != cudaSuccess) return cuda_fail(h, e, "flux buffer upload");
@@ -866,9 +868,13 @@ extern "C" int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, d
   if (h->mhd)
     return fail(h, MHD_ERR_INVALID, "Flux corrections are currently only supported in hydro-mode");
   for (int d = 0; d < 3; d++)
-    for (int sd = 0; sd < 2; sd++)
+    for (int sd = 0; sd < 2; sd++) {
       if (fc->flux[d][sd][MHD_Q_INTERNAL_ENERGY] && !h->de)
         return fail(h, MHD_ERR_INVALID, "internal_energy fluxes need dual energy");
+      for (int k = b->npassive; k < 4; k++)
+        if (fc->flux[d][sd][MHD_Q_PASSIVE_0 + k])
+          return fail(h, MHD_ERR_INVALID, "a passive-scalar flux names a scalar the block lacks");
+    }
   cudaStream_t st = (cudaStream_t)stream;
   return b->dtype == MHD_DTYPE_F64 ? block_step_t<double>(h, b, dt, nullptr, fc, st)
                                    : block_step_t<float>(h, b, dt, nullptr, fc, st);

@@ -32,7 +32,7 @@ using namespace mhdint;
 
 namespace {
 
-constexpr int NQ = 6;  // MHD_Q_*
+constexpr int NQ = MHD_FC_NQ;  // MHD_Q_*: six hydro quantities, four passive scalars
 constexpr int FC_CHUNK = 256;
 
 // one corrected face of a coarse block
@@ -48,9 +48,10 @@ struct FcChunk {
   int face, start;
 };
 
-// per-block device pointers: the six corrected fields and the stored fluxes
+// per-block device pointers: the corrected fields and the stored fluxes
 struct FcBlockPtrs {
-  void* field[NQ];          // density, velocity_x/y/z, total_energy, internal_energy
+  void* field[NQ];          // density, velocity_x/y/z, total_energy, internal_energy,
+                            // passive scalars 0-3 (conserved form)
   void* flux[3][2][NQ];
 };
 
@@ -199,6 +200,8 @@ int plan_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks
     for (int a = 0; a < 3; a++) p.field[MHD_Q_VELOCITY_X + a] = b.velocity[a];
     p.field[MHD_Q_TOTAL_ENERGY] = b.total_energy;
     p.field[MHD_Q_INTERNAL_ENERGY] = b.internal_energy;
+    for (int k = 0; k < 4; k++)
+      p.field[MHD_Q_PASSIVE_0 + k] = k < b.npassive ? b.passive[k] : nullptr;
     for (int a = 0; a < 3; a++)
       for (int s = 0; s < 2; s++)
         for (int q = 0; q < NQ; q++) {
@@ -212,14 +215,16 @@ int plan_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks
   }
   if (((qmask >> 1) & 7u) != 0 && ((qmask >> 1) & 7u) != 7u)
     return fail(h, MHD_ERR_INVALID, "store all three momentum fluxes or none");
-  // the conservative mask in MHD_Q_* bits (field slots 1..5 are the same)
+  // the conservative mask in MHD_Q_* bits (field slots 1..5 are the same;
+  // the passive scalars' field slots start at MHD_FIELD_PASSIVE_0).  Without
+  // a stored density flux a density-weighted field is divided by the
+  // uncorrected density, as the reference does.
   P.qmask = qmask;
   P.cons = 0;
-  for (int q = 1; q < NQ; q++)
+  for (int q = 1; q < MHD_Q_PASSIVE_0; q++)
     if ((conservative >> q) & 1u) P.cons |= 1u << q;
-  if ((P.cons & qmask) && !(qmask & 1u)) {
-    // the reference divides by the (uncorrected) density then; allowed
-  }
+  for (int k = 0; k < 4; k++)
+    if ((conservative >> (MHD_FIELD_PASSIVE_0 + k)) & 1u) P.cons |= 1u << (MHD_Q_PASSIVE_0 + k);
   // corrected faces: (coarse block, axis, face) <- four finer children
   std::vector<int> index((size_t)nblocks * 6, -1);
   std::vector<FcFace> fl;

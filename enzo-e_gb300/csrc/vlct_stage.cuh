@@ -459,7 +459,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     auto store_fluxes = [&](int t, bool zfaces, int pl) {
       const FluxOut<R>* fo = static_cast<const FluxOut<R>*>(B.fc != nullptr ? B.fc : info.fc);
       const int gg = info.fc_g;
-      auto put = [&](int d, int side, size_t at, const R* f) {
+      // f: the face's hydro fluxes; pf: its first passive-scalar flux (the
+      // scalars follow G apart)
+      auto put = [&](int d, int side, size_t at, const R* f, const R* pf) {
         const R sc = dtdx[d];
 #pragma unroll
         for (int q = 0; q < 6; q++) {
@@ -470,6 +472,14 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
                     : q == 4 ? f[S_E * G] : (DE ? f[S_EINT * G] : R(0));
           p[at] = sc * v;
         }
+        for (int k = 0; k < NP; k++) {
+          R* p = fo->f[d][side][6 + k];
+          if (p) p[at] = sc * pf[k * G];
+        }
+      };
+      // the passive fluxes of direction d in ring slot sl (phase B's layout)
+      auto pflux = [&](int d, int sl, int r) {
+        return sm + Ls.o_pf + (size_t)((d * 2 + sl) * NP) * G + r;
       };
       const int xlo = xa > gg ? xa : gg, xhi = xb < m0 - gg ? xb : m0 - gg;
       const int ylo = ya > gg ? ya : gg, yhi = yb < m1 - gg ? yb : m1 - gg;
@@ -479,14 +489,18 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         for (int side = 0; side < 2; side++) {
           const int x = side == 0 ? gg - 1 : m0 - gg - 1;  // x faces
           if (x >= xa - 1 && x < xb - 1)
-            for (int y = ylo + tid; y < yhi; y += nthr)
-              put(0, side, (size_t)(pl - gg) * (m1 - 2 * gg) + (y - gg),
-                  xf + (y - hy0) * HP + (x - hx0));
+            for (int y = ylo + tid; y < yhi; y += nthr) {
+              const int r = (y - hy0) * HP + (x - hx0);
+              put(0, side, (size_t)(pl - gg) * (m1 - 2 * gg) + (y - gg), xf + r,
+                  pflux(0, pl & 1, r));
+            }
           const int y = side == 0 ? gg - 1 : m1 - gg - 1;  // y faces
           if (y >= ya - 1 && y < yb - 1)
-            for (int x2 = xlo + tid; x2 < xhi; x2 += nthr)
-              put(1, side, (size_t)(pl - gg) * (m0 - 2 * gg) + (x2 - gg),
-                  yf + (y - hy0) * HP + (x2 - hx0));
+            for (int x2 = xlo + tid; x2 < xhi; x2 += nthr) {
+              const int r = (y - hy0) * HP + (x2 - hx0);
+              put(1, side, (size_t)(pl - gg) * (m0 - 2 * gg) + (x2 - gg), yf + r,
+                  pflux(1, pl & 1, r));
+            }
         }
       }
       const int side = t == gg - 1 ? 0 : (t == m2 - gg - 1 ? 1 : -1);  // z faces at t+1/2
@@ -495,8 +509,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         const int w = xhi - xlo;
         for (int k = tid; k < w * (yhi - ylo); k += nthr) {
           const int y = ylo + k / w, x = xlo + k % w;
-          put(2, side, (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg),
-              zf + (y - hy0) * HP + (x - hx0));
+          const int r = (y - hy0) * HP + (x - hx0);
+          put(2, side, (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg), zf + r,
+              pflux(2, t & 1, r));
         }
       }
     };

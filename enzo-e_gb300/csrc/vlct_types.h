@@ -71,12 +71,14 @@ struct StageInfo {
 
 // Boundary fluxes for flux correction (EnzoMethodMHDVlct.cpp:250-330):
 // f[dim][side][q] receives dt/dx_dim times the flux of quantity q (0 density,
-// 1-3 velocity x/y/z, 4 total energy, 5 internal energy) through the low
+// 1-3 velocity x/y/z, 4 total energy, 5 internal energy, 6-9 passive
+// scalars 0-3 in conserved form) through the low
 // (side 0, face g-1) or high (side 1, face m-g-1) active face of axis dim,
 // as an array of the active face, last index fastest: axis 0 (nz, ny),
 // axis 1 (nz, nx), axis 2 (ny, nx).  Null pointers are skipped.
+constexpr int kFluxQuantities = 10;  // MHD_FC_NQ of the C interface
 template <class R> struct FluxOut {
-  R* f[3][2][6];
+  R* f[3][2][kFluxQuantities];  // [axis][side][MHD_Q_*]
   int g;
 };
 

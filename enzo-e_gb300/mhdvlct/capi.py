@@ -63,11 +63,13 @@ class MhdVlctParams(ctypes.Structure):
 
 class MhdFluxCorrection(ctypes.Structure):
     """flux[axis][side][quantity]: device arrays of the active boundary faces."""
-    _fields_ = [("flux", ctypes.c_void_p * 6 * 2 * 3)]
+    _fields_ = [("flux", ctypes.c_void_p * 10 * 2 * 3)]
 
 
 MHD_Q_DENSITY, MHD_Q_VELOCITY_X, MHD_Q_VELOCITY_Y, MHD_Q_VELOCITY_Z = 0, 1, 2, 3
 MHD_Q_TOTAL_ENERGY, MHD_Q_INTERNAL_ENERGY = 4, 5
+MHD_Q_PASSIVE_0 = 6  # .. 9: the passive scalars (conserved form)
+MHD_FC_NQ = 10
 
 MHD_REFRESH_COARSE, MHD_REFRESH_SAME, MHD_REFRESH_FINE = -1, 0, 1
 # field slots of the mesh refresh (MHD_FIELD_* in the header)
@@ -77,6 +79,7 @@ FIELD_SLOTS = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energ
                "passive_1", "passive_2", "passive_3", "bfieldi_x", "bfieldi_y",
                "bfieldi_z")
 MHD_NFIELD_SLOTS = len(FIELD_SLOTS)
+MHD_FIELD_PASSIVE_0 = FIELD_SLOTS.index("passive_0")
 MHD_CONSERVATIVE_DEFAULT = sum(1 << FIELD_SLOTS.index(k) for k in (
     "velocity_x", "velocity_y", "velocity_z", "total_energy"))
 

@@ -132,17 +132,24 @@ int mhdvlct_block_step(mhdvlct_handle* h, const MhdBlockView* b, double dt,
  * flux[axis][side][quantity] is a device array of the block's active face in
  * the block's dtype, last index fastest: axis 0 (nz, ny), axis 1 (nz, nx),
  * axis 2 (ny, nx); NULL entries are skipped.  Hydro only (the reference
- * asserts it); internal_energy needs dual energy. */
+ * asserts it); internal_energy needs dual energy.  The passive scalars'
+ * fluxes (their conserved-form flux: the density flux times the upwind
+ * specific scalar) are stored like any other field of the flux-correction
+ * group, as the reference's FluxData holds every field of its "conserved"
+ * group (EnzoMethodMHDVlct.cpp:265-272): MHD_Q_PASSIVE_0 + k needs
+ * npassive > k. */
 enum {
   MHD_Q_DENSITY = 0,
   MHD_Q_VELOCITY_X = 1, /* the x-momentum flux, as the reference keys it */
   MHD_Q_VELOCITY_Y = 2,
   MHD_Q_VELOCITY_Z = 3,
   MHD_Q_TOTAL_ENERGY = 4,
-  MHD_Q_INTERNAL_ENERGY = 5
+  MHD_Q_INTERNAL_ENERGY = 5,
+  MHD_Q_PASSIVE_0 = 6,  /* .. MHD_Q_PASSIVE_0 + 3: MhdBlockView::passive[k] */
+  MHD_FC_NQ = 10
 };
 typedef struct MhdFluxCorrection {
-  void* flux[3][2][6];
+  void* flux[3][2][MHD_FC_NQ];
 } MhdFluxCorrection;
 int mhdvlct_block_step_fc(mhdvlct_handle* h, const MhdBlockView* b, double dt,
                           const MhdFluxCorrection* fc, void* stream);
@@ -288,7 +295,9 @@ int mhdvlct_refresh_faces(mhdvlct_handle* h, const MhdBlockView* blocks, int nbl
  * quantities.  faces: the mesh's refresh faces (mhdvlct_refresh_faces); the
  * axis faces of type MHD_REFRESH_COARSE are the ones used.  Cell fields
  * updated: density, velocity_x/y/z (momentum fluxes), total_energy,
- * internal_energy, as stored. */
+ * internal_energy and the passive scalars, as stored; a passive scalar in
+ * the `conservative` mask (bit MHD_FIELD_PASSIVE_0 + k) is corrected as a
+ * density-weighted value like the velocities. */
 int mhdvlct_flux_correct(mhdvlct_handle* h, const MhdBlockView* blocks, int nblocks,
                          const MhdFluxCorrection* fluxes, const MhdRefreshFace* faces,
                          int nfaces, unsigned conservative, void* stream);
@@ -346,7 +355,8 @@ int mhdvlct_batch_set_refresh_faces(mhdvlct_batch* b, const MhdRefreshFace* face
  * stage of every cycle and apply the flux correction of the mesh `faces`
  * (see mhdvlct_flux_correct) right after it, inside the cycle's CUDA graph:
  * the reference's Method list ["mhd_vlct", "flux_correct"].  Hydro only;
- * blocks of equal extents.  quantities = 0 turns it off. */
+ * blocks of equal extents; bit MHD_Q_PASSIVE_0 + k needs the batch's
+ * npassive > k.  quantities = 0 turns it off. */
 int mhdvlct_batch_set_flux_correction(mhdvlct_batch* b, unsigned quantities,
                                       const MhdRefreshFace* faces, int nfaces,
                                       unsigned conservative);

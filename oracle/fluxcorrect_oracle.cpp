@@ -20,7 +20,10 @@
 
 namespace {
 
-const int NQ = 6;  // density, velocity_x/y/z, total_energy, internal_energy
+// density, velocity_x/y/z, total_energy, internal_energy, passive scalars 0-3
+// (every field of the reference's flux-correction group,
+// src/Cello/problem_MethodFluxCorrect.cpp:55-77)
+const int NQ = 10;
 
 template <class T>
 T* fluxp(void* const* fluxes, int blk, int axis, int side, int q) {
@@ -176,8 +179,9 @@ int flux_correct(int nblocks, const int n[3], const int g[3], void* const* field
 
 }  // namespace
 
-/* fields: nblocks x 6 pointers (density, velocity_x/y/z, total_energy,
- * internal_energy; NULL = absent); fluxes: nblocks x 3 x 2 x 6 pointers of the
+/* fields: nblocks x 10 pointers (density, velocity_x/y/z, total_energy,
+ * internal_energy, passive scalars 0-3; NULL = absent); cons: bits of the
+ * same slots; fluxes: nblocks x 3 x 2 x 10 pointers of the
  * stored boundary fluxes (axis, side, quantity); faces: 9 ints each (the mesh
  * refresh faces); dtype 0 = double, 1 = float. */
 extern "C" int oracle_flux_correct(int dtype, int nblocks, const int n[3], const int g[3],

@@ -229,7 +229,8 @@ def step(prm: OracleParams, b: Block, dt: float, ref: bool = False) -> None:
 
 
 FC_QUANTITIES = ("density", "velocity_x", "velocity_y", "velocity_z",
-                 "total_energy", "internal_energy")
+                 "total_energy", "internal_energy",
+                 "passive_0", "passive_1", "passive_2", "passive_3")
 
 
 def step_fc(prm: OracleParams, b: Block, dt: float, quantities=(0, 1, 2, 3, 4),
@@ -445,17 +446,17 @@ def flux_correct(blocks, fluxes, n, g, faces, cons: int) -> None:
     """Correct in place.  blocks: list of dicts MHD_Q index -> array;
     fluxes: list of dicts (axis, side, q) -> stored flux array (as step_fc
     returns them); faces: int array of 9 per face."""
-    nb = len(blocks)
-    fp = (ctypes.c_void_p * (6 * nb))()
-    xp = (ctypes.c_void_p * (36 * nb))()
+    nb, nq = len(blocks), len(FC_QUANTITIES)
+    fp = (ctypes.c_void_p * (nq * nb))()
+    xp = (ctypes.c_void_p * (6 * nq * nb))()
     dt = None
     for i, b in enumerate(blocks):
         for q, a in b.items():
             dt = a.dtype if dt is None else dt
-            fp[6 * i + q] = a.ctypes.data
+            fp[nq * i + q] = a.ctypes.data
         for (ax, side, q), a in fluxes[i].items():
             assert a.flags.c_contiguous and a.dtype == dt
-            xp[36 * i + (ax * 2 + side) * 6 + q] = a.ctypes.data
+            xp[6 * nq * i + (ax * 2 + side) * nq + q] = a.ctypes.data
     faces = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 9)
     rc = lib().oracle_flux_correct(0 if dt == np.float64 else 1, nb, _i3(n), _i3(g), fp, xp,
                                    faces.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),

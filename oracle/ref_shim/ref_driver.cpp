@@ -140,8 +140,9 @@ struct Scratch {
 static void save_fc(const std::array<EnzoEFltArrayMap, 3>& flux_maps, int g,
                     const int cc[3], const double cw[3], double dt,
                     double* const* out, int nq, const int* quantities) {
-  static const char* names[6] = {"density", "velocity_x", "velocity_y",
-                                 "velocity_z", "total_energy", "internal_energy"};
+  static const char* names[10] = {"density", "velocity_x", "velocity_y",
+                                  "velocity_z", "total_energy", "internal_energy",
+                                  "pass0", "pass1", "pass2", "pass3"};
   const int n[3] = {cc[0] - 2 * g, cc[1] - 2 * g, cc[2] - 2 * g};
   for (int dim = 0; dim < 3; dim++) {
     const double dt_dxi = dt / cw[dim];

@@ -1043,7 +1043,9 @@ extern "C" long long oracle_flop_count(void) { return g_flops; }
 // requested integration quantities.  out[(dim * 2 + side) * nq + iq] holds an
 // array of the block's active face, last index fastest: axis 0 (nz, ny),
 // axis 1 (nz, nx), axis 2 (ny, nx).  quantities: 0 density, 1-3 velocity
-// x/y/z (the momentum flux), 4 total energy, 5 internal energy.
+// x/y/z (the momentum flux), 4 total energy, 5 internal energy, 6-9 passive
+// scalars 0-3 (the conserved-form flux: FluxData holds every field of the
+// "conserved" group, EnzoMethodMHDVlct.cpp:265-272).
 static void save_boundary_fluxes(const Ctx& c, const Scratch& sc, double dt,
                                  const double* cw, int g, double* const* out,
                                  int nq, const int* quantities) {
@@ -1053,7 +1055,8 @@ static void save_boundary_fluxes(const Ctx& c, const Scratch& sc, double dt,
     const double dt_dxi = dt / cw[dim];
     for (int iq = 0; iq < nq; iq++) {
       const int q = quantities[iq];
-      const V3 F = (q == 5) ? sc.eflux[dim].w
+      const V3 F = (q >= 6) ? sc.pflux[dim][q - 6].w
+                 : (q == 5) ? sc.eflux[dim].w
                  : (q == 0) ? sc.flux[dim][Q_RHO].w
                  : (q == 4) ? sc.flux[dim][Q_P].w
                             : sc.flux[dim][Q_VX + (q - 1)].w;
@@ -1092,8 +1095,9 @@ extern "C" int oracle_step(const OracleParams* p, OracleBlock* b, double dt) {
 extern "C" int oracle_step_fc(const OracleParams* p, OracleBlock* b, double dt,
                               double* const* out, int nq, const int* quantities) {
   if (p->mhd) return 4;
+  const int np = std::max(0, std::min(b->npassive, NPASS));
   for (int i = 0; i < nq; i++)
-    if (quantities[i] < 0 || quantities[i] > 5 ||
+    if (quantities[i] < 0 || quantities[i] >= 6 + np ||
         (quantities[i] == 5 && !p->dual_energy))
       return 5;
   return step_impl(p, b, dt, out, nq, quantities);

@@ -7,7 +7,11 @@ reference's own FaceFluxes::coarsen in tests/test_flux_correct_oracle.py):
     the oracle's run bit for bit in FP64 and conserves mass, momentum and
     total energy to round-off;
   - the FP32 correction alone equals the oracle's FP32 restatement bit for
-    bit on random fields and fluxes.
+    bit on random fields and fluxes;
+  - with passive scalars in the flux-correction group (Cello corrects every
+    field of its group, src/Cello/problem_MethodFluxCorrect.cpp:55-77), the
+    per-block and the batched (graph-replayed) runs equal the oracle's bit
+    for bit in FP64 and conserve each scalar's mass to round-off.
 """
 import numpy as np
 import pytest
@@ -15,7 +19,7 @@ import torch
 
 from oracle import oracle as O
 from mhdvlct import block as B, capi, mesh as M
-from test_flux_correct_oracle import smr_blocks, totals
+from test_flux_correct_oracle import fc_fields, smr_blocks, smr_slots, totals
 
 pytestmark = pytest.mark.gpu
 
@@ -187,3 +191,91 @@ def test_batch_fp32_with_flux_correction_close_to_fp64_oracle():
             want = ob.f[o][act]
             err = np.abs(got[k][act].astype(np.float64) - want).sum() / np.abs(want).sum()
             assert err <= 1e-5, (i, k, err)
+
+
+NPASS = 2
+PNAMES = tuple(f"passive_{k}" for k in range(NPASS))
+PONAMES = tuple(f"pass{k}" for k in range(NPASS))
+PQS = (0, 1, 2, 3, 4) + tuple(capi.MHD_Q_PASSIVE_0 + k for k in range(NPASS))
+
+
+def _oracle_passive_run(mesh, oblocks, n, g, cycles, cons):
+    prm = O.params(riemann=O.HLLC, recon=O.PLM, mhd=False, courant=0.4)
+    faces = mesh.face_ints()
+    slots = [smr_slots(b, NPASS) for b in oblocks]
+    fields = [fc_fields(b, NPASS) for b in oblocks]
+    O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+    dts = []
+    for _ in range(cycles):
+        dt = min(O.timestep(prm, b) for b in oblocks)
+        O.refresh_faces(slots, (n,) * 3, (g,) * 3, faces, cons)
+        fl = [O.step_fc(prm, b, dt, quantities=PQS) for b in oblocks]
+        O.flux_correct(fields, fl, (n,) * 3, (g,) * 3, faces, cons)
+        dts.append(dt)
+    return dts
+
+
+def test_smr_passive_per_block_bit_exact_and_conservative():
+    n, g, cycles = 8, 4, 2
+    mesh, oblocks, vols = smr_blocks(n, g, npassive=NPASS)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    blocks = []
+    for ob in oblocks:
+        b = B.Block((n,) * 3, g, ob.widths, mhd=False, npassive=NPASS)
+        b.load_numpy({k: ob.f[o] for k, o in zip(NAMES + PNAMES, ONAMES + PONAMES)})
+        blocks.append(b)
+    bufs = [B.FluxBuffers(b, PQS) for b in blocks]
+    faces = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    t0 = None
+    meth.refresh_faces(blocks, faces, cons)
+    for _ in range(cycles):
+        dt = min(meth.timestep(b) for b in blocks)
+        meth.refresh_faces(blocks, faces, cons)
+        for b, buf in zip(blocks, bufs):
+            meth.compute_store_fluxes(b, dt, PQS, buffers=buf)
+        meth.flux_correct(blocks, bufs, faces, cons)
+    torch.cuda.synchronize()
+    # the oracle's run from the same initial state
+    _, ob0, _ = smr_blocks(n, g, npassive=NPASS)
+    O.refresh_faces([smr_slots(b, NPASS) for b in ob0], (n,) * 3, (g,) * 3,
+                    mesh.face_ints(), cons)
+    t0 = totals(ob0, vols, n, g, NPASS)
+    _oracle_passive_run(mesh, oblocks, n, g, cycles, cons)
+    for i, (b, ob) in enumerate(zip(blocks, oblocks)):
+        got = b.to_numpy()
+        for k, o in zip(NAMES + PNAMES, ONAMES + PONAMES):
+            assert np.array_equal(got[k], ob.f[o]), (i, k)
+    t1 = totals(oblocks, vols, n, g, NPASS)
+    assert float((np.abs(t1 - t0) / np.abs(t0)).max()) < 1e-15
+
+
+def test_batch_graph_passive_flux_correction_bit_exact():
+    from test_gpu_batch import Batch
+    n, g, cycles = 8, 4, 3
+    mesh, oblocks, vols = smr_blocks(n, g, npassive=NPASS)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    L = capi.lib()
+    bt = Batch(meth, [(n,) * 3] * len(oblocks), [ob.widths for ob in oblocks], ghost=g,
+               npassive=NPASS)
+    for i, ob in enumerate(oblocks):
+        bt.upload(i, {k: ob.f[o] for k, o in zip(NAMES + PNAMES, ONAMES + PONAMES)})
+    farr, nf = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    qmask = sum(1 << q for q in PQS)
+    capi.check(L.mhdvlct_batch_set_refresh_faces(bt.h, farr, nf, cons), meth.handle, "faces")
+    # a scalar the batch lacks is refused
+    assert L.mhdvlct_batch_set_flux_correction(
+        bt.h, qmask | (1 << (capi.MHD_Q_PASSIVE_0 + NPASS)), farr, nf,
+        cons) == capi.MHD_ERR_INVALID
+    capi.check(L.mhdvlct_batch_set_flux_correction(bt.h, qmask, farr, nf, cons),
+               meth.handle, "flux correction")
+    capi.check(L.mhdvlct_batch_refresh(bt.h, None), meth.handle, "refresh")
+    capi.check(L.mhdvlct_batch_run(bt.h, cycles, 0, None, None), meth.handle, "run")
+    _oracle_passive_run(mesh, oblocks, n, g, cycles, cons)
+    for i, ob in enumerate(oblocks):
+        got = bt.download(i)
+        for k, o in zip(NAMES + PNAMES, ONAMES + PONAMES):
+            assert np.array_equal(got[k], ob.f[o]), (i, k)

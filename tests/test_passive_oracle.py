@@ -66,3 +66,33 @@ def test_passive_scalar_mass_is_advected():
     g = G
     act = (slice(g, g + N[2]), slice(g, g + N[1]), slice(g, g + N[0]))
     np.testing.assert_allclose(a.f["pass0"][act] / a.f["rho"][act], 0.25, rtol=1e-12)
+
+
+@pytest.mark.skipif(O.ref_lib() is None, reason="reference sources not built here")
+@pytest.mark.parametrize("recon,de", [("plm", False), ("nn", True)])
+def test_oracle_passive_boundary_fluxes_match_reference(recon, de):
+    """store_fluxes_for_corrections with the passive scalars in the
+    flux-correction group: the reference keys FluxData by field name and
+    stores every field of the group (EnzoMethodMHDVlct.cpp:265-272), so each
+    scalar's conserved-form boundary flux is saved beside the hydro ones."""
+    a, b = _blocks(False, de, 29, npass=3)
+    prm = oracle_params("hllc", recon, de=de, courant=0.3)
+    dt = O.timestep(prm, a)
+    assert O.timestep(prm, b, ref=True) == dt
+    qs = (0, 1, 2, 3, 4) + ((5,) if de else ()) + (6, 7, 8)
+    fa = O.step_fc(prm, a, dt, quantities=qs)
+    fb = O.step_fc(prm, b, dt, quantities=qs, ref=True)
+    assert fa.keys() == fb.keys()
+    for key in fa:
+        assert np.array_equal(fa[key], fb[key]), key
+        if key[2] >= 6:
+            assert np.count_nonzero(fa[key]) > 0, key
+    for k in a.f:
+        assert np.array_equal(a.f[k], b.f[k]), k
+
+
+def test_oracle_step_fc_rejects_missing_scalar():
+    a, _ = _blocks(False, False, 31, npass=1)
+    prm = oracle_params("hllc", "plm", courant=0.3)
+    with pytest.raises(RuntimeError):
+        O.step_fc(prm, a, 1e-3, quantities=(0, 7))
