@@ -63,6 +63,8 @@ struct mhdvlct_batch {
     size_t ext[NCELL], tmp[NCELL], fa[3], fb[3], tf[3], pres;
     size_t pas[4], ptmp[4], acc[3];  // passive scalars (state, half step),
                                      // acceleration; (size_t)-1 when absent
+    size_t dfl[3];                   // with passive scalars: the stages'
+                                     // density fluxes (scratch)
     int m[3];
   };
   std::vector<Off> off;
@@ -165,8 +167,8 @@ TileChoice choice_for(const mhdvlct_batch* b, int i) {
   const StagePlan sp = stage_plan(b->h);
   for (int s = 0; s < 2; s++)
     if (c.tile_x[s] <= 0 || c.tile_y[s] <= 0) {
-      const int t = default_tile(b->dtype, b->h->solver, sp.recon[s], b->h->de, b->npass);
-      c.tile_x[s] = c.tile_y[s] = t;
+      default_tile_xy(b->dtype, b->h->solver, sp.recon[s], b->h->de, c.tile_x[s],
+                      c.tile_y[s]);
     }
   if (!tuned) {
     // untuned default: when the batch has too few column tiles to fill the
@@ -243,6 +245,7 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
           B.pass_cur[k] = s == 0 ? ep : tp;
           B.pass_out[k] = s == 0 ? tp : ep;
         }
+        for (int d = 0; d < 3; d++) B.dflux[d] = b->npass > 0 ? b->ptr<R>(O.dfl[d]) : nullptr;
         if (s == 0) {
           B.cur = cur_faces;
           B.out = tmp;
@@ -499,6 +502,8 @@ int mhdint::batch_create(mhdvlct_handle* h, const int* dims, const double* width
       }
       for (int d = 0; d < 3; d++)
         if (pass == 0) O.acc[d] = gravity ? take(M) : (size_t)-1;
+      for (int d = 0; d < 3; d++)
+        if (pass == 1) O.dfl[d] = npassive > 0 ? take(M) : (size_t)-1;
       for (int d = 0; d < 3; d++)
         if (pass == 1) O.tf[d] = h->mhd ? take(F[d]) : (size_t)-1;
       if (pass == 1) O.pres = take(M);
@@ -1215,8 +1220,7 @@ int autotune_t(mhdvlct_batch* b, int reps, std::string& json, cudaStream_t st) {
       std::vector<TileChoice> cands;
       for (auto& sh : shapes) {
         if (stage_smem<R>(b->h->solver, sp.recon[s], b->h->de != 0,
-                          std::max(sh.first, other_tx), std::max(sh.second, other_ty),
-                          b->npass) >
+                          std::max(sh.first, other_tx), std::max(sh.second, other_ty)) >
             smem_cap)
           continue;
         for (int zc : {0, 16}) {

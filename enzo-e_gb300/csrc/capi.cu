@@ -105,24 +105,35 @@ FieldSet<R> fieldset_of(const MhdBlockView* b) {
 template FieldSet<double> fieldset_of<double>(const MhdBlockView*);
 template FieldSet<float> fieldset_of<float>(const MhdBlockView*);
 
-int default_tile(int dtype, int solver, int recon, int de, int np) {
-  // largest tile whose shared memory (np passive scalars included) fits the
-  // CTAs an SM holds at once (227 KB per SM): one CTA for FP64, three for
-  // the FP32 NN stage, two for the other FP32 stages
-  // (the NN stage that carries passive scalars is compiled for two CTAs)
-  const int cap = (dtype == MHD_DTYPE_F64)         ? 200 * 1024
-                  : (recon == RECON_NN && np == 0) ? 72 * 1024
-                                                   : 110 * 1024;
+int default_tile(int dtype, int solver, int recon, int de) {
+  // largest square tile whose shared memory fits the CTAs an SM holds at
+  // once (227 KB per SM): one CTA for FP64, three for the FP32 NN stage, two
+  // for the other FP32 stages
+  const int cap = (dtype == MHD_DTYPE_F64) ? 200 * 1024
+                  : (recon == RECON_NN)    ? 72 * 1024
+                                           : 110 * 1024;
   int best = 4;
   for (int t = 4; t <= (dtype == MHD_DTYPE_F64 ? TileLimits<double>::TMAX
                                                  : TileLimits<float>::TMAX);
        t++) {
     const size_t b = (dtype == MHD_DTYPE_F64)
-                         ? stage_smem<double>(solver, recon, de != 0, t, t, np)
-                         : stage_smem<float>(solver, recon, de != 0, t, t, np);
+                         ? stage_smem<double>(solver, recon, de != 0, t, t)
+                         : stage_smem<float>(solver, recon, de != 0, t, t);
     if (b <= (size_t)cap) best = t;
   }
   return best;
+}
+
+void default_tile_xy(int dtype, int solver, int recon, int de, int& tx, int& ty) {
+  if (dtype == MHD_DTYPE_F32) {
+    // the shapes the autotuner settles on for 32^3 blocks: wide in x
+    // (coalesced rows), one large tile per SM; the tile split evens them
+    // out over other block sizes.  Both fit 227 KB with dual energy.
+    tx = recon == RECON_NN ? 34 : 24;
+    ty = recon == RECON_NN ? 10 : 16;
+    return;
+  }
+  tx = ty = default_tile(dtype, solver, recon, de);
 }
 
 }  // namespace mhdint
@@ -526,14 +537,13 @@ int sm_count() {
   }();
   return n;
 }
-PlainDecomp plain_decomp(const mhdvlct_handle* h, const int m[3], int dtype, int np) {
+PlainDecomp plain_decomp(const mhdvlct_handle* h, const int m[3], int dtype) {
   PlainDecomp d;
   const StagePlan sp = stage_plan(h);
   for (int i = 0; i < sp.nstages; i++) {
     const bool final = i + 1 == sp.nstages;
-    const int tmax = default_tile(dtype, h->solver, sp.recon[i], h->de, np);
-    const int per_sm = dtype == MHD_DTYPE_F64 ? 1
-                       : (sp.recon[i] == RECON_NN && np == 0) ? 3 : 2;
+    const int tmax = default_tile(dtype, h->solver, sp.recon[i], h->de);
+    const int per_sm = dtype == MHD_DTYPE_F64 ? 1 : (sp.recon[i] == RECON_NN) ? 3 : 2;
     const long resident = (long)per_sm * sm_count();
     double best = 1e300;
     for (int t = std::min(6, tmax); t <= tmax; t++) {
@@ -563,6 +573,7 @@ PlainDecomp plain_decomp(const mhdvlct_handle* h, const int m[3], int dtype, int
 template <class R> struct PlainScratch {
   R* tmp[NCELL];
   R* tpass[4];               // half-step passive scalars
+  R* dflux[3];               // with passive scalars: the stages' density fluxes
   R* tface[3];
   R* fface[3];
   double* d_dt;
@@ -583,7 +594,7 @@ template <class R>
 int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
                    PlainScratch<R>& S, cudaStream_t st, int np = 0) {
   const StagePlan sp = stage_plan(h);
-  const PlainDecomp dc = plain_decomp(h, m, dtype, np);
+  const PlainDecomp dc = plain_decomp(h, m, dtype);
   TileSplit ts[2] = {};
   long nt[2] = {0, 0};
   for (int i = 0; i < sp.nstages; i++) {
@@ -601,6 +612,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   for (int d = 0; d < 3; d++) take(F[d] * sizeof(R));
   for (int d = 0; d < 3; d++) take(F[d] * sizeof(R));
   for (int k = 0; k < np; k++) take(M * sizeof(R));
+  for (int d = 0; d < 3 && np > 0; d++) take(M * sizeof(R));
   take(sizeof(double));
   take(sizeof(double));
   take(3 * sizeof(unsigned long long));
@@ -634,6 +646,7 @@ int ensure_scratch(mhdvlct_handle* h, const int m[3], int dtype,
   for (int d = 0; d < 3; d++) S.tface[d] = (R*)(base + offs[i++]);
   for (int d = 0; d < 3; d++) S.fface[d] = (R*)(base + offs[i++]);
   for (int k = 0; k < 4; k++) S.tpass[k] = k < np ? (R*)(base + offs[i++]) : nullptr;
+  for (int d = 0; d < 3; d++) S.dflux[d] = np > 0 ? (R*)(base + offs[i++]) : nullptr;
   S.d_dt = (double*)(base + offs[i++]);
   S.d_dtout = (double*)(base + offs[i++]);
   S.d_smax = (void*)(base + offs[i++]);
@@ -698,6 +711,7 @@ int block_step_on(mhdvlct_handle* h, const MhdBlockView* b, PlainScratch<R>& S,
       B.pass_cur[k] = (sp.nstages == 1 || i == 1) ? S.tpass[k] : ep;
       B.pass_out[k] = (sp.nstages == 2 && i == 0) ? S.tpass[k] : ep;
     }
+    for (int d = 0; d < 3; d++) B.dflux[d] = np > 0 ? S.dflux[d] : nullptr;
     if (sp.nstages == 1) {
       // euler: a single stage cannot update its own input in place, so it
       // reads a copy of the block and writes into the caller's fields
@@ -996,7 +1010,7 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   const StagePlan sp = stage_plan(h);
   const int np = b->npassive;
   // the same work decomposition as mhdvlct_block_step
-  const PlainDecomp dc = plain_decomp(h, m, b->dtype, np);
+  const PlainDecomp dc = plain_decomp(h, m, b->dtype);
   TileSplit ts[2] = {};
   long nt[2] = {0, 0};
   for (int i = 0; i < sp.nstages; i++) {
@@ -1021,9 +1035,10 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
     off += align_up(bytes);
     return o;
   };
-  size_t o_tmp[NCELL], o_tf[3], o_ff[3], o_tp[4];
+  size_t o_tmp[NCELL], o_tf[3], o_ff[3], o_tp[4], o_df[3];
   for (int k = 0; k < NCELL; k++) o_tmp[k] = take(M * sizeof(R));
   for (int k = 0; k < np; k++) o_tp[k] = take(M * sizeof(R));  // half-step scalars
+  for (int d = 0; d < 3 && np > 0; d++) o_df[d] = take(M * sizeof(R));  // density fluxes
   for (int d = 0; d < 3; d++) o_tf[d] = take(F[d] * sizeof(R));
   for (int d = 0; d < 3; d++) o_ff[d] = take(F[d] * sizeof(R));
   const size_t o_dt = take(sizeof(double));
@@ -1042,6 +1057,7 @@ int block_step_noalloc_t(mhdvlct_handle* h, const MhdBlockView* b, double dt,
   PlainScratch<R> S{};
   for (int k = 0; k < NCELL; k++) S.tmp[k] = (R*)(base + o_tmp[k]);
   for (int k = 0; k < 4; k++) S.tpass[k] = k < np ? (R*)(base + o_tp[k]) : nullptr;
+  for (int d = 0; d < 3; d++) S.dflux[d] = np > 0 ? (R*)(base + o_df[d]) : nullptr;
   for (int d = 0; d < 3; d++) {
     S.tface[d] = (R*)(base + o_tf[d]);
     S.fface[d] = (R*)(base + o_ff[d]);

@@ -60,7 +60,9 @@ template <class R>
 vlct::FieldSet<R> fieldset_of(const MhdBlockView* b);
 
 // Default tile extent for a precision (fits the shared-memory budget).
-int default_tile(int dtype, int solver, int recon, int de, int np = 0);
+int default_tile(int dtype, int solver, int recon, int de);
+// Default tile shape of the batched form (tx x ty columns).
+void default_tile_xy(int dtype, int solver, int recon, int de, int& tx, int& ty);
 
 // The batched form (batch.cu).  batch_create is mhdvlct_batch_create_ex with,
 // when ordered_stream is not null, every device allocation, free and set-up

@@ -5,6 +5,7 @@
 
 #include "vlct_aux.cuh"
 #include "vlct_launch.h"
+#include "vlct_passive.cuh"
 #include "vlct_stage.cuh"
 
 namespace vlct {
@@ -16,8 +17,7 @@ cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
                       cudaStream_t st) {
   const bool all = info.gravity != 0 || info.npass > 0;
   const bool fc = info.fc != nullptr || info.block_fc != 0;
-  const size_t smem =
-      stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty, all ? info.npass : 0);
+  const size_t smem = stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty);
   // the flux-storing-only variant exists for the hydro solver (flux
   // correction is hydro only); the others take the full variant
   auto k = all ? stage_kernel<R, SOLVER, RECON, DE, EXTRA_ALL>
@@ -44,7 +44,14 @@ cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
   }
   if (grid > nt) grid = nt;
   k<<<grid, threads, smem, st>>>(b, t, nt, info, phys);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  // the passive scalars, on the same tiles, with the density fluxes the
+  // stage kernel wrote
+  if (e == cudaSuccess && info.npass > 0) {
+    passive_kernel<R, RECON><<<nt, 256, 0, st>>>(b, t, info, phys);
+    e = cudaGetLastError();
+  }
+  return e;
 }
 
 template <class R, int SOLVER, bool DE>
@@ -69,11 +76,11 @@ cudaError_t stage_de(int recon, bool de, const StageBlock<R>* b,
 }
 
 template <class R, int SOLVER, bool DE>
-size_t smem_recon(int recon, int tx, int ty, int np) {
+size_t smem_recon(int recon, int tx, int ty) {
   switch (recon) {
-    case RECON_NN: return stage_smem_bytes<R, SOLVER, RECON_NN, DE>(tx, ty, np);
-    case RECON_PLM: return stage_smem_bytes<R, SOLVER, RECON_PLM, DE>(tx, ty, np);
-    default: return stage_smem_bytes<R, SOLVER, RECON_PLM_ATHENA, DE>(tx, ty, np);
+    case RECON_NN: return stage_smem_bytes<R, SOLVER, RECON_NN, DE>(tx, ty);
+    case RECON_PLM: return stage_smem_bytes<R, SOLVER, RECON_PLM, DE>(tx, ty);
+    default: return stage_smem_bytes<R, SOLVER, RECON_PLM_ATHENA, DE>(tx, ty);
   }
 }
 }  // namespace
@@ -94,14 +101,14 @@ cudaError_t launch_stage<VLCT_REAL>(int solver, int recon, bool de,
 }
 
 template <>
-size_t stage_smem<VLCT_REAL>(int solver, int recon, bool de, int tx, int ty, int np) {
+size_t stage_smem<VLCT_REAL>(int solver, int recon, bool de, int tx, int ty) {
   // the solver changes only NF (hydro vs MHD)
   if (solver == SOLVER_HLLC) {
-    return de ? smem_recon<VLCT_REAL, SOLVER_HLLC, true>(recon, tx, ty, np)
-              : smem_recon<VLCT_REAL, SOLVER_HLLC, false>(recon, tx, ty, np);
+    return de ? smem_recon<VLCT_REAL, SOLVER_HLLC, true>(recon, tx, ty)
+              : smem_recon<VLCT_REAL, SOLVER_HLLC, false>(recon, tx, ty);
   }
-  return de ? smem_recon<VLCT_REAL, SOLVER_HLLD, true>(recon, tx, ty, np)
-            : smem_recon<VLCT_REAL, SOLVER_HLLD, false>(recon, tx, ty, np);
+  return de ? smem_recon<VLCT_REAL, SOLVER_HLLD, true>(recon, tx, ty)
+            : smem_recon<VLCT_REAL, SOLVER_HLLD, false>(recon, tx, ty);
 }
 
 template <>

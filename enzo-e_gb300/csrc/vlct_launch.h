@@ -23,7 +23,7 @@ cudaError_t launch_stage(int solver, int recon, bool de,
                          const PhysParams& phys, int grid, cudaStream_t st);
 
 template <class R>
-size_t stage_smem(int solver, int recon, bool de, int tx, int ty, int np = 0);
+size_t stage_smem(int solver, int recon, bool de, int tx, int ty);
 
 template <class R>
 cudaError_t launch_timestep(bool mhd, bool de, const AuxBlock<R>* d_blocks,

@@ -29,8 +29,10 @@
 // (total minus kinetic minus magnetic energy) and the energy floor / sync run
 // in float-float (vlct_energy.cuh).  Further instantiations (EXTRA) also
 // store the boundary fluxes for flux correction (EXTRA_FC) or, in addition,
-// add the gravity source and advect passive scalars (EXTRA_ALL); the default
-// one compiles all of these out.
+// add the gravity source and write the density flux of every updated face
+// for the passive scalars' advection (EXTRA_ALL; the scalars themselves are
+// advected by passive_kernel, vlct_passive.cuh); the default one compiles
+// all of these out.
 #pragma once
 #include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
@@ -84,9 +86,8 @@ struct SmemLayout {
   int HP, HQ;   // halo grid pitch / rows (tile + 1 cell each side)
   int G;        // HP * HQ
   int o_prim, o_xf, o_yf, o_zf, o_ec, o_ex, o_ey, o_ez, o_bz;
-  int o_pprim, o_pf;  // passive scalars: specific-form ring, face fluxes
   int total;    // in elements of R
-  __host__ __device__ void init(int tx, int ty, int rp, int nring, int nf, int np = 0) {
+  __host__ __device__ void init(int tx, int ty, int rp, int nring, int nf) {
     PP = tx + 2 + 2 * rp;
     QP = ty + 2 + 2 * rp;
     HP = tx + 2;
@@ -102,17 +103,15 @@ struct SmemLayout {
     o_ey = o; o += 2 * G;
     o_ez = o; o += G;
     o_bz = o; o += 2 * G;
-    o_pprim = o; o += nring * np * PP * QP;
-    o_pf = o; o += 3 * 2 * np * G;  // [dir][slot][scalar]
     total = o;
   }
 };
 
 template <class R, int SOLVER, int RECON, bool DE>
-size_t stage_smem_bytes(int tx, int ty, int np = 0) {
+size_t stage_smem_bytes(int tx, int ty) {
   using C = StageCfg<R, SOLVER, RECON, DE>;
   SmemLayout L;
-  L.init(tx, ty, C::RP, C::NRING, C::NF, np);
+  L.init(tx, ty, C::RP, C::NRING, C::NF);
   return (size_t)L.total * sizeof(R);
 }
 
@@ -146,13 +145,11 @@ enum { EXTRA_NONE = 0, EXTRA_FC = 1, EXTRA_ALL = 2 };
 
 // EXTRA: EXTRA_NONE compiles the optional work out (its run-time checks alone
 // cost ~4% of a stage); EXTRA_FC can store the boundary fluxes; EXTRA_ALL
-// can also add the gravity source and advect passive scalars (their code
-// paths cost a further ~20% of a stage even when idle).
+// can also add the gravity source and write the density fluxes that
+// passive_kernel advects the passive scalars with.
 template <class R, int SOLVER, int RECON, bool DE, int EXTRA>
 __global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
-                                  (EXTRA == EXTRA_ALL && StageBounds<R, RECON>::min_blocks > 2)
-                                      ? 2
-                                      : StageBounds<R, RECON>::min_blocks)
+                                  StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
              const StageTile* __restrict__ tiles, int ntiles, StageInfo info,
              PhysParams phys) {
@@ -162,9 +159,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
   SmemLayout Ls;
-  // passive scalars exist only in the EXTRA_ALL instantiation
-  const int NP = EXTRA == EXTRA_ALL ? info.npass : 0;
-  Ls.init(info.tx, info.ty, RP, NRING, NF, NP);
+  Ls.init(info.tx, info.ty, RP, NRING, NF);
+  // passive scalars (EXTRA_ALL only) are advected by passive_kernel after
+  // this kernel, with the density flux of every face written here
   const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;
   const int PQ = PP * QP;
   R* s_prim = sm + Ls.o_prim;
@@ -190,6 +187,11 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   // tile: read from global memory, its field pointers would be reloaded after
   // every global store (the compiler cannot rule out aliasing)
   __shared__ __align__(16) unsigned long long s_blk_raw[(sizeof(StageBlock<R>) + 7) / 8];
+  // the block's flux-correction outputs on a flux-storing final stage, also
+  // copied once per tile: read from global memory, every boundary-face store
+  // would first wait for its pointer
+  constexpr int kFoWords = EXTRA != EXTRA_NONE ? (int)((sizeof(FluxOut<R>) + 7) / 8) : 1;
+  __shared__ __align__(16) unsigned long long s_fo_raw[kFoWords];
   __shared__ R s_dtdx[3];
   __shared__ R s_dt;
   int it = blockIdx.x;
@@ -205,6 +207,11 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           reinterpret_cast<const unsigned long long*>(blocks + tl.block);
       for (int w = tid; w < (int)((sizeof(StageBlock<R>) + 7) / 8); w += nthr)
         s_blk_raw[w] = src[w];
+      if (EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc)) {
+        const void* fsrc = blocks[tl.block].fc != nullptr ? blocks[tl.block].fc : info.fc;
+        const unsigned long long* fw = reinterpret_cast<const unsigned long long*>(fsrc);
+        for (int w = tid; w < kFoWords; w += nthr) s_fo_raw[w] = fw[w];
+      }
     }
     const StageBlock<R>& B = *reinterpret_cast<const StageBlock<R>*>(s_blk_raw);
     const StageBlock<R>& Bg = blocks[tl.block];
@@ -273,9 +280,6 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           w[(Q_BX + 2) * PQ] = bz;
         }
         w[Q_P * PQ] = p_out;
-        // passive scalars in specific form (EnzoPhysicsFluidProps.cpp:120-133)
-        for (int k = 0; k < NP; k++)
-          sm[Ls.o_pprim + (slot * NP + k) * PQ + poff(0, x, y)] = B.pass_cur[k][c] / rho;
         // cell-centred E = -v x B (EnzoBfieldMethodCT.cpp:267-292), on the
         // halo grid and inside [S, m - S)
         const int hi = x - hx0, hj = y - hy0;
@@ -312,7 +316,6 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         const int x = hx0 + i, y = hy0 + j;
         // face index f along d: the face between cells f and f+1
         int off[4];  // s_prim offsets of the cells f-1 .. f+2 along d
-        int sl[4];   // their ring slots (for the passive planes' offsets)
         const R* bface;
         R* dst;
         const int r = j * HP + i;
@@ -321,10 +324,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           if (!inr(fz, S, m2 - 1 - S) || !inr(x, S, m0 - S) || !inr(y, S, m1 - S))
             continue;
 #pragma unroll
-          for (int k = 0; k < 4; k++) {
-            sl[k] = (fz - 1 + k + NRING) % NRING;
-            off[k] = poff(sl[k], x, y);
-          }
+          for (int k = 0; k < 4; k++) off[k] = poff((fz - 1 + k + NRING) % NRING, x, y);
           bface = B.cur.f[2] + ((size_t)(fz + 1) * cstr_z + (size_t)y * cstr_y + x);
           dst = s_zf + (size_t)(fz & 1) * NF * G + r;
         } else {
@@ -333,20 +333,14 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           if (d == 0) {
             if (!inr(x, S, m0 - 1 - S) || !inr(y, S, m1 - S)) continue;
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-              sl[k] = slot;
-              off[k] = poff(slot, x - 1 + k, y);
-            }
+            for (int k = 0; k < 4; k++) off[k] = poff(slot, x - 1 + k, y);
             bface = B.cur.f[0] + ((size_t)pl * ((size_t)m1 * (m0 + 1)) +
                                   (size_t)y * (m0 + 1) + (x + 1));
             dst = s_xf + (size_t)(pl & 1) * NF * G + r;
           } else {
             if (!inr(y, S, m1 - 1 - S) || !inr(x, S, m0 - S)) continue;
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-              sl[k] = slot;
-              off[k] = poff(slot, x, y - 1 + k);
-            }
+            for (int k = 0; k < 4; k++) off[k] = poff(slot, x, y - 1 + k);
             bface = B.cur.f[1] + ((size_t)pl * ((size_t)(m1 + 1) * m0) +
                                   (size_t)(y + 1) * m0 + x);
             dst = s_yf + (size_t)(pl & 1) * NF * G + r;
@@ -412,37 +406,6 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           dst[S_EINT * G] = F.eflux;
           dst[S_VBAR * G] = F.vbar;
         }
-        // passive scalars (EnzoRiemannUtils.hpp:224-314): reconstruct the
-        // specific scalar like the primitives (no floor), flux = upwind value
-        // times the density flux; stored beside the face's other fluxes
-        for (int k = 0; k < NP; k++) {
-          const R* w = sm + Ls.o_pprim + k * PQ;
-          // cell j of the stencil: ring slot sl[j] holds NP passive planes
-          // instead of NQ primitive planes, at the same in-plane position
-          const int dq = (NP - NQ) * PQ;
-          auto at = [&](int j) { return w[off[j] + sl[j] * dq]; };
-          R lv, rv;
-          if (RECON == RECON_NN) {
-            lv = at(1);
-            rv = at(2);
-          } else {
-            const R a = at(0), b0 = at(1), b1 = at(2), c = at(3);
-            R dl, dr;
-            if (RECON == RECON_PLM) {
-              dl = limiter_enzo_rk(a, b0, b1, theta);
-              dr = limiter_enzo_rk(b0, b1, c, theta);
-            } else {
-              dl = limiter_athena(a, b0, b1);
-              dr = limiter_athena(b0, b1, c);
-            }
-            lv = b0 + dl * R(0.5);
-            rv = b1 - dr * R(0.5);
-          }
-          const R df = F.f[L_RHO];
-          const R upwind = ((df > R(0)) ? R(1) : R(0)) * lv + ((df <= R(0)) ? R(1) : R(0)) * rv;
-          const int pslot = (d == 2) ? (t & 1) : (pl & 1);
-          sm[Ls.o_pf + ((d * 2 + pslot) * NP + k) * G + r] = upwind * df;
-        }
       }
     };
 
@@ -457,11 +420,11 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     const bool store_fc =
         EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc);
     auto store_fluxes = [&](int t, bool zfaces, int pl) {
-      const FluxOut<R>* fo = static_cast<const FluxOut<R>*>(B.fc != nullptr ? B.fc : info.fc);
+      const FluxOut<R>* fo = reinterpret_cast<const FluxOut<R>*>(s_fo_raw);
       const int gg = info.fc_g;
-      // f: the face's hydro fluxes; pf: its first passive-scalar flux (the
-      // scalars follow G apart)
-      auto put = [&](int d, int side, size_t at, const R* f, const R* pf) {
+      // f: the face's fluxes (the passive scalars' are stored by
+      // passive_kernel)
+      auto put = [&](int d, int side, size_t at, const R* f) {
         const R sc = dtdx[d];
 #pragma unroll
         for (int q = 0; q < 6; q++) {
@@ -472,14 +435,6 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
                     : q == 4 ? f[S_E * G] : (DE ? f[S_EINT * G] : R(0));
           p[at] = sc * v;
         }
-        for (int k = 0; k < NP; k++) {
-          R* p = fo->f[d][side][6 + k];
-          if (p) p[at] = sc * pf[k * G];
-        }
-      };
-      // the passive fluxes of direction d in ring slot sl (phase B's layout)
-      auto pflux = [&](int d, int sl, int r) {
-        return sm + Ls.o_pf + (size_t)((d * 2 + sl) * NP) * G + r;
       };
       const int xlo = xa > gg ? xa : gg, xhi = xb < m0 - gg ? xb : m0 - gg;
       const int ylo = ya > gg ? ya : gg, yhi = yb < m1 - gg ? yb : m1 - gg;
@@ -491,15 +446,13 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           if (x >= xa - 1 && x < xb - 1)
             for (int y = ylo + tid; y < yhi; y += nthr) {
               const int r = (y - hy0) * HP + (x - hx0);
-              put(0, side, (size_t)(pl - gg) * (m1 - 2 * gg) + (y - gg), xf + r,
-                  pflux(0, pl & 1, r));
+              put(0, side, (size_t)(pl - gg) * (m1 - 2 * gg) + (y - gg), xf + r);
             }
           const int y = side == 0 ? gg - 1 : m1 - gg - 1;  // y faces
           if (y >= ya - 1 && y < yb - 1)
             for (int x2 = xlo + tid; x2 < xhi; x2 += nthr) {
               const int r = (y - hy0) * HP + (x2 - hx0);
-              put(1, side, (size_t)(pl - gg) * (m0 - 2 * gg) + (x2 - gg), yf + r,
-                  pflux(1, pl & 1, r));
+              put(1, side, (size_t)(pl - gg) * (m0 - 2 * gg) + (x2 - gg), yf + r);
             }
         }
       }
@@ -510,8 +463,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
         for (int k = tid; k < w * (yhi - ylo); k += nthr) {
           const int y = ylo + k / w, x = xlo + k % w;
           const int r = (y - hy0) * HP + (x - hx0);
-          put(2, side, (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg), zf + r,
-              pflux(2, t & 1, r));
+          put(2, side, (size_t)(y - gg) * (m0 - 2 * gg) + (x - gg), zf + r);
         }
       }
     };
@@ -722,18 +674,17 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           B.out.c[F_VZ][c] = vz;
           B.out.c[F_ETOT][c] = etot;
           if (DE) B.out.c[F_EINT][c] = eint;
-          // update_passive_scalars_ (EnzoIntegrationQuanUpdate.cpp:242-270):
-          // conserved = start-of-step + dU
-          for (int k = 0; k < NP; k++) {
-            const R* fx = sm + Ls.o_pf + ((0 * 2 + (t & 1)) * NP + k) * G;
-            const R* fy = sm + Ls.o_pf + ((1 * 2 + (t & 1)) * NP + k) * G;
-            const R* fzp = sm + Ls.o_pf + ((2 * 2 + (t & 1)) * NP + k) * G;
-            const R* fzm = sm + Ls.o_pf + ((2 * 2 + ((t - 1) & 1)) * NP + k) * G;
-            R a = R(0.0);
-            a -= dtdx[0] * (fx[r] - fx[r - 1]);
-            a -= dtdx[1] * (fy[r] - fy[r - HP]);
-            a -= dtdx[2] * (fzp[r] - fzm[r]);
-            B.pass_out[k][c] = B.pass_base[k][c] + a;
+          // the passive scalars' advection (passive_kernel) needs the
+          // density flux of both faces of every updated cell along each
+          // axis: the low faces here, the high faces at the region's edges
+          if (EXTRA == EXTRA_ALL && info.npass > 0) {
+            R* const* D = B.dflux;
+            D[0][c] = xf0[S_RHO * G + r - 1];
+            D[1][c] = yf0[S_RHO * G + r - HP];
+            D[2][c] = zfm[S_RHO * G + r];
+            if (x + 1 == m0 - S - 1) D[0][c + 1] = xf0[S_RHO * G + r];
+            if (y + 1 == m1 - S - 1) D[1][c + cstr_y] = yf0[S_RHO * G + r];
+            if (t + 1 == m2 - S - 1) D[2][c + cstr_z] = zfp[S_RHO * G + r];
           }
         }
       }

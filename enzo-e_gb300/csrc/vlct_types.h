@@ -30,6 +30,11 @@ template <class R> struct StageBlock {
   const R* pass_cur[4] = {nullptr, nullptr, nullptr, nullptr};
   const R* pass_base[4] = {nullptr, nullptr, nullptr, nullptr};
   R* pass_out[4] = {nullptr, nullptr, nullptr, nullptr};
+  // with passive scalars: per axis d, the density flux through the low
+  // d-face of every cell the stage updates (and through the high face of the
+  // last cell), written by the stage kernel for passive_kernel; cell-shaped
+  // arrays of the ghosted block
+  R* dflux[3] = {nullptr, nullptr, nullptr};
   // FluxOut<R> (device) of this block on the final stage when a batch stores
   // the boundary fluxes for flux correction; null otherwise
   const void* fc = nullptr;
