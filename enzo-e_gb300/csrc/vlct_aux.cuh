@@ -73,41 +73,61 @@ timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
   R* __restrict__ const f_etot = B.f.c[F_ETOT];
   R* __restrict__ const f_eint = B.f.c[F_EINT];
   R* __restrict__ const f_p = B.pressure;
-#pragma unroll 4
-  for (size_t c = (size_t)chunk * blockDim.x + threadIdx.x; c < ncell;
-       c += (size_t)chunks_per_block * blockDim.x) {
-    const R rho = f_rho[c];
-    const R vx = f_vx[c], vy = f_vy[c], vz = f_vz[c];
-    R bx = R(0), by = R(0), bz = R(0);
-    if (MHD) {
-      bx = f_bx[c];
-      by = f_by[c];
-      bz = f_bz[c];
+  // U cells per thread per pass, every load of the pass issued before the
+  // arithmetic (the pass's stores would otherwise hold later loads back)
+  constexpr int U = 4;
+  const size_t stride = (size_t)chunks_per_block * blockDim.x;
+  for (size_t c0 = (size_t)chunk * blockDim.x + threadIdx.x; c0 < ncell; c0 += U * stride) {
+    R rho[U], vx[U], vy[U], vz[U], bx[U], by[U], bz[U], et[U], ei[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const size_t c = c0 + u * stride;
+      const bool ok = c < ncell;
+      const size_t cc = ok ? c : c0;  // a valid index; the result is unused
+      rho[u] = f_rho[cc];
+      vx[u] = f_vx[cc];
+      vy[u] = f_vy[cc];
+      vz[u] = f_vz[cc];
+      bx[u] = by[u] = bz[u] = R(0);
+      if (MHD) {
+        bx[u] = f_bx[cc];
+        by[u] = f_by[cc];
+        bz[u] = f_bz[cc];
+      }
+      et[u] = f_etot[cc];
+      ei[u] = DE ? f_eint[cc] : R(0);
     }
-    R p;
-    if (DE) {
-      // apply_floor_to_energy_and_sync over the whole block (stale depth 0)
-      R etot = f_etot[c], eint = f_eint[c];
-      energy_floor_sync<MHD, true>(econ, rho, vx, vy, vz, bx, by, bz, etot, eint);
-      f_eint[c] = eint;
-      f_etot[c] = etot;
-      p = econ.gm1 * rho * eint;
-    } else {
-      p = pressure_from_etot<R, MHD>(econ, rho, f_etot[c], vx, vy, vz, bx, by, bz);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const size_t c = c0 + u * stride;
+      if (c >= ncell) break;
+      R p;
+      if (DE) {
+        // apply_floor_to_energy_and_sync over the whole block (stale depth 0)
+        R etot = et[u], eint = ei[u];
+        energy_floor_sync<MHD, true>(econ, rho[u], vx[u], vy[u], vz[u], bx[u], by[u], bz[u],
+                                     etot, eint);
+        f_eint[c] = eint;
+        f_etot[c] = etot;
+        p = econ.gm1 * rho[u] * eint;
+      } else {
+        p = pressure_from_etot<R, MHD>(econ, rho[u], et[u], vx[u], vy[u], vz[u], bx[u], by[u],
+                                       bz[u]);
+      }
+      if (f_p) f_p[c] = p;
+      R cf;
+      if (MHD) {  // fast_magnetosonic_speed<0> (EnzoEOSIdeal.hpp:124-126)
+        const R B2 = sqmag(bx[u], by[u], bz[u]);
+        const R c2 = cs2(g, rho[u], p);
+        const R va2 = B2 / rho[u];
+        cf = sqrt(va2 + c2);
+      } else {
+        cf = sqrt(cs2(g, rho[u], p));
+      }
+      s[0] = fmax(s[0], fabs(vx[u]) + cf);
+      s[1] = fmax(s[1], fabs(vy[u]) + cf);
+      s[2] = fmax(s[2], fabs(vz[u]) + cf);
     }
-    if (f_p) f_p[c] = p;
-    R cf;
-    if (MHD) {  // fast_magnetosonic_speed<0> (EnzoEOSIdeal.hpp:124-126)
-      const R B2 = sqmag(bx, by, bz);
-      const R c2 = cs2(g, rho, p);
-      const R va2 = B2 / rho;
-      cf = sqrt(va2 + c2);
-    } else {
-      cf = sqrt(cs2(g, rho, p));
-    }
-    s[0] = fmax(s[0], fabs(vx) + cf);
-    s[1] = fmax(s[1], fabs(vy) + cf);
-    s[2] = fmax(s[2], fabs(vz) + cf);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -329,8 +349,9 @@ refresh_shell_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restri
     const int cy = iz * wy * e[0];
     const int cx = iz * iy * wx;
     const int total = cz + cy + cx;
-    for (int q = chunk * blockDim.x + threadIdx.x; q < total;
-         q += chunks_per_block * blockDim.x) {
+    // the destination and source index of shell cell q (and the source's
+    // neighbour slot k)
+    auto locate = [&](int q, size_t& di, size_t& si, int& k) {
       int x, y, z;
       if (q < cz) {
         const int r1 = mdiv(q, e[0], m0);
@@ -365,14 +386,46 @@ refresh_shell_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restri
         side[a] = (i < g) ? -1 : ((i >= hi[a]) ? 1 : 0);
         src[a] = i - side[a] * n[a];
       }
-      const int k = (side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1);
-      const size_t di = ((size_t)z * e[1] + y) * e[0] + x;
-      const size_t si = ((size_t)src[2] * e[1] + src[1]) * e[0] + src[0];
-      if (face < 0) {
-#pragma unroll 4
-        for (int j = 0; j < nc; j++) s_dst[j][di] = s_src[j][k][si];
-      } else {
-        s_fdst[face][di] = s_fsrc[face][k][si];
+      k = (side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1);
+      di = ((size_t)z * e[1] + y) * e[0] + x;
+      si = ((size_t)src[2] * e[1] + src[1]) * e[0] + src[0];
+    };
+    const int stride = chunks_per_block * blockDim.x;
+    if (face < 0) {
+      // every field of a cell: all loads issued before any store (through
+      // the pointer tables the compiler cannot rule out aliasing, and would
+      // otherwise wait out one memory round trip per field)
+      for (int q = chunk * blockDim.x + threadIdx.x; q < total; q += stride) {
+        size_t di, si;
+        int k;
+        locate(q, di, si, k);
+        R v[NC];
+#pragma unroll
+        for (int j = 0; j < NC; j++)
+          if (j < nc) v[j] = s_src[j][k][si];
+#pragma unroll
+        for (int j = 0; j < NC; j++)
+          if (j < nc) s_dst[j][di] = v[j];
+      }
+    } else {
+      // one field: four cells' loads in flight per thread
+      constexpr int U = 4;
+      for (int q0 = chunk * blockDim.x + threadIdx.x; q0 < total; q0 += U * stride) {
+        size_t di[U];
+        R v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int q = q0 + u * stride;
+          if (q < total) {
+            size_t si;
+            int k;
+            locate(q, di[u], si, k);
+            v[u] = s_fsrc[face][k][si];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (q0 + u * stride < total) s_fdst[face][di[u]] = v[u];
       }
     }
   }
