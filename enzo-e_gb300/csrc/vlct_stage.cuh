@@ -17,7 +17,8 @@
 //      plane t -- centred B, flux divergence + dual-energy source, density
 //      floor, energy floor / dual-energy sync, store -- and the primitives
 //      + cell-centred E of plane t+1+L (L = 1 for NN, 2 for PLM) loaded into
-//      the ring for the next plane.
+//      the ring for the next plane (in the PLM stages the raw fields are
+//      copied asynchronously right after B and converted here).
 //
 // The index windows of every quantity are those of the reference's array
 // passes (EnzoMHDIntegratorStageCommands::compute_update_stage,
@@ -47,6 +48,25 @@ enum { S_RHO = 0, S_MX = 1, S_E = 4, S_BJ = 5, S_BK = 6, S_EINT = 7, S_VBAR = 8 
 
 __device__ __forceinline__ bool inr(int a, int lo, int hi) {
   return a >= lo && a < hi;
+}
+
+// Asynchronous global -> shared copy of one element (cp.async, cached in
+// L1), and the calls that close a group of them and wait for the calling
+// thread's own copies.
+template <class R>
+__device__ __forceinline__ void cp_async_elem(R* smem, const R* gmem) {
+  static_assert(sizeof(R) == 4 || sizeof(R) == 8, "element size");
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if (sizeof(R) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 // Upwind weight of CT from the sign of the density flux
@@ -244,40 +264,80 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
       return slot * NQ * PQ + (y - py0) * PP + (x - px0);
     };
 
-    // ---- primitives (and the cell-centred E) of plane p into its ring slot
-    auto load_plane = [&](int p) {
-      if (!inr(p, s, m2 - s)) return;
+    // ---- primitives (and the cell-centred E) of plane p into its ring slot,
+    // in two steps.  With ASYNC_LOADS (the PLM stages) issue_plane starts
+    // asynchronous copies of the raw cell fields into the slot (the energy
+    // field into the pressure plane) and finish_plane, after the copies have
+    // landed, turns them into primitives in place.  Every thread finishes
+    // exactly the cells it issued, so the two need no barrier between them;
+    // in the z-march the copies of plane t+1+L go out right after phase B of
+    // plane t (the slot they overwrite, plane t-1's, is no longer read) and
+    // land while phases C and D run.  The NN stage, already close to its
+    // issue limit, loads in finish_plane directly: the extra shared-memory
+    // pass costs it more than the latency it would hide.
+    constexpr bool ASYNC_LOADS = RECON != RECON_NN;
+    auto issue_plane = [&](int p) {
+      if (!ASYNC_LOADS || !inr(p, s, m2 - s)) return;
       const int slot = p % NRING;
+      const int fe = DE ? F_EINT : F_ETOT;
       for (int idx = tid; idx < PQ; idx += nthr) {
         const int qy = divPP.div(idx);
         const int x = px0 + (idx - qy * PP), y = py0 + qy;
         if (!inr(x, s, m0 - s) || !inr(y, s, m1 - s)) continue;
         const size_t c = (size_t)p * cstr_z + (size_t)y * cstr_y + x;
-        const R rho = B.cur.c[F_RHO][c];
-        const R vx = B.cur.c[F_VX][c], vy = B.cur.c[F_VY][c], vz = B.cur.c[F_VZ][c];
+        R* w = s_prim + poff(slot, x, y);
+        cp_async_elem(w + Q_RHO * PQ, B.cur.c[F_RHO] + c);
+        cp_async_elem(w + (Q_VX + 0) * PQ, B.cur.c[F_VX] + c);
+        cp_async_elem(w + (Q_VX + 1) * PQ, B.cur.c[F_VY] + c);
+        cp_async_elem(w + (Q_VX + 2) * PQ, B.cur.c[F_VZ] + c);
+        if (MHD) {
+          cp_async_elem(w + (Q_BX + 0) * PQ, B.cur.c[F_BX] + c);
+          cp_async_elem(w + (Q_BX + 1) * PQ, B.cur.c[F_BY] + c);
+          cp_async_elem(w + (Q_BX + 2) * PQ, B.cur.c[F_BZ] + c);
+        }
+        cp_async_elem(w + Q_P * PQ, B.cur.c[fe] + c);
+      }
+      cp_async_commit();
+    };
+    auto finish_plane = [&](int p) {
+      if (!inr(p, s, m2 - s)) return;
+      if (ASYNC_LOADS) cp_async_wait_all();
+      const int slot = p % NRING;
+      const int fe = DE ? F_EINT : F_ETOT;
+      for (int idx = tid; idx < PQ; idx += nthr) {
+        const int qy = divPP.div(idx);
+        const int x = px0 + (idx - qy * PP), y = py0 + qy;
+        if (!inr(x, s, m0 - s) || !inr(y, s, m1 - s)) continue;
+        R* w = s_prim + poff(slot, x, y);
+        const size_t c = (size_t)p * cstr_z + (size_t)y * cstr_y + x;
+        // the fields: from the slot (copied there) or from global memory
+        auto field = [&](int q, int f) -> R { return ASYNC_LOADS ? w[q * PQ] : B.cur.c[f][c]; };
+        const R rho = field(Q_RHO, F_RHO);
+        const R vx = field(Q_VX + 0, F_VX), vy = field(Q_VX + 1, F_VY), vz = field(Q_VX + 2, F_VZ);
         R bx = R(0), by = R(0), bz = R(0);
         if (MHD) {
-          bx = B.cur.c[F_BX][c];
-          by = B.cur.c[F_BY][c];
-          bz = B.cur.c[F_BZ][c];
+          bx = field(Q_BX + 0, F_BX);
+          by = field(Q_BX + 1, F_BY);
+          bz = field(Q_BX + 2, F_BZ);
+        }
+        // EnzoComputePressure::compute_pressure (EnzoComputePressure.cpp:127-190)
+        const R e_in = field(Q_P, fe);
+        if (!ASYNC_LOADS) {
+          w[Q_RHO * PQ] = rho;
+          w[(Q_VX + 0) * PQ] = vx;
+          w[(Q_VX + 1) * PQ] = vy;
+          w[(Q_VX + 2) * PQ] = vz;
+          if (MHD) {
+            w[(Q_BX + 0) * PQ] = bx;
+            w[(Q_BX + 1) * PQ] = by;
+            w[(Q_BX + 2) * PQ] = bz;
+          }
         }
         R p_out;
-        // EnzoComputePressure::compute_pressure (EnzoComputePressure.cpp:127-190)
         if (DE) {
-          p_out = econ.gm1 * rho * B.cur.c[F_EINT][c];
+          p_out = econ.gm1 * rho * e_in;
         } else {
-          p_out = pressure_from_etot<R, MHD>(econ, rho, B.cur.c[F_ETOT][c], vx, vy, vz,
-                                             bx, by, bz);
-        }
-        R* w = s_prim + poff(slot, x, y);
-        w[Q_RHO * PQ] = rho;
-        w[(Q_VX + 0) * PQ] = vx;
-        w[(Q_VX + 1) * PQ] = vy;
-        w[(Q_VX + 2) * PQ] = vz;
-        if (MHD) {
-          w[(Q_BX + 0) * PQ] = bx;
-          w[(Q_BX + 1) * PQ] = by;
-          w[(Q_BX + 2) * PQ] = bz;
+          p_out = pressure_from_etot<R, MHD>(econ, rho, e_in, vx, vy, vz, bx, by, bz);
         }
         w[Q_P * PQ] = p_out;
         // cell-centred E = -v x B (EnzoBfieldMethodCT.cpp:267-292), on the
@@ -469,7 +529,8 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     };
 
     // ---------------------------------------------------------- prologue --
-    for (int p = t0 - (LOOK - 1); p <= t0 + LOOK; p++) load_plane(p);
+    for (int p = t0 - (LOOK - 1); p <= t0 + LOOK; p++) issue_plane(p);
+    for (int p = t0 - (LOOK - 1); p <= t0 + LOOK; p++) finish_plane(p);
     __syncthreads();
     phase_b(t0 - 1, false, t0);
     __syncthreads();
@@ -479,6 +540,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
       // ---- B: z-faces at t+1/2, x/y faces of plane t+1
       phase_b(t, true, t + 1);
       __syncthreads();
+      // plane t+1+L's fields start towards the ring slot phase B just
+      // released (plane t-1's)
+      if (t + 1 < zb) issue_plane(t + 1 + LOOK);
       if (store_fc) store_fluxes(t, true, t + 1);
       // ---- C: edge EMFs (EnzoBfieldMethodCT.cpp:480-590)
       if (MHD) {
@@ -536,7 +600,8 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
       // not updated in this stage keeps its start-of-step value.  Bz at t+1
       // stays in shared memory for the same column's next plane, so the
       // mapping of columns to threads is the same for every plane.  The
-      // primitives of plane t+1+LOOK load into the ring in the same phase.
+      // primitives of plane t+1+LOOK are finished into the ring in the same
+      // phase.
       {
         const bool do_plane = t >= za;
         // the lowest face of a chunk is written by the chunk below it
@@ -688,7 +753,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           }
         }
       }
-      if (t + 1 < zb) load_plane(t + 1 + LOOK);
+      if (t + 1 < zb) finish_plane(t + 1 + LOOK);
       __syncthreads();
     }
     // next tile: dynamic queue (persistent grid) or static grid stride
