@@ -389,7 +389,7 @@ cudaError_t launch_timestep_b(mhdvlct_batch* b, int global_min, cudaStream_t st)
   for (auto& o : b->off) cells += (size_t)o.m[0] * o.m[1] * o.m[2];
   const size_t per = std::max<size_t>(1, cells / b->nblocks);
   const int cpb = (int)std::max<size_t>(
-      1, std::min<size_t>(per / 2048, std::max<size_t>(64, fill_ctas() / b->nblocks)));
+      1, std::min<size_t>(per / 8192, std::max<size_t>(64, fill_ctas() / b->nblocks)));
   return launch_timestep<R>(b->h->mhd != 0, b->h->de != 0,
                             (const AuxBlock<R>*)b->d_aux[b->parity], b->nblocks, cpb,
                             b->h->phys, b->d_smax, b->h->params.courant, global_min,

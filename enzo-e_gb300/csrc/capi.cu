@@ -353,6 +353,7 @@ extern "C" int mhdvlct_create(const MhdVlctParams* p, mhdvlct_handle** out) {
   h->phys.pressure_floor = p->pressure_floor;
   h->phys.theta_limiter = p->theta_limiter;
   h->phys.eta = h->de ? p->dual_energy_eta : 0.0;
+  h->phys.set_derived();
   *out = h;
   return MHD_OK;
 }

@@ -2,6 +2,8 @@
 // reduction, the same-level ghost refresh gather, the FP64 conserved-total /
 // div B diagnostics and small copy helpers.
 #pragma once
+#include <type_traits>
+
 #include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
 #include "vlct_types.h"
@@ -57,7 +59,7 @@ timestep_kernel(const AuxBlock<R>* __restrict__ blocks, int nblocks,
   const size_t ncell = (size_t)B.m[0] * B.m[1] * B.m[2];
   const R g = R(phys.gamma);
   EnergyConsts<R> econ;
-  econ.init(phys.gamma, phys.pressure_floor, DE ? phys.eta : 0.0);
+  econ.init(phys, DE);
   R s[3] = {R(0), R(0), R(0)};
   // the block's field pointers in registers: the descriptor lives in global
   // memory, and the stores below would otherwise force a reload per cell
@@ -394,18 +396,39 @@ refresh_shell_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restri
     if (face < 0) {
       // every field of a cell: all loads issued before any store (through
       // the pointer tables the compiler cannot rule out aliasing, and would
-      // otherwise wait out one memory round trip per field)
-      for (int q = chunk * blockDim.x + threadIdx.x; q < total; q += stride) {
-        size_t di, si;
-        int k;
-        locate(q, di, si, k);
-        R v[NC];
+      // otherwise wait out one memory round trip per field); the loop is
+      // compiled for the block's exact field count
+      auto copy_cells = [&](auto count) {
+        constexpr int N = decltype(count)::value;
+        for (int q = chunk * blockDim.x + threadIdx.x; q < total; q += stride) {
+          size_t di, si;
+          int k;
+          locate(q, di, si, k);
+          R v[N];
 #pragma unroll
-        for (int j = 0; j < NC; j++)
-          if (j < nc) v[j] = s_src[j][k][si];
+          for (int j = 0; j < N; j++) v[j] = s_src[j][k][si];
 #pragma unroll
-        for (int j = 0; j < NC; j++)
-          if (j < nc) s_dst[j][di] = v[j];
+          for (int j = 0; j < N; j++) s_dst[j][di] = v[j];
+        }
+      };
+      switch (nc) {
+        case 1: copy_cells(std::integral_constant<int, 1>{}); break;
+        case 2: copy_cells(std::integral_constant<int, 2>{}); break;
+        case 3: copy_cells(std::integral_constant<int, 3>{}); break;
+        case 4: copy_cells(std::integral_constant<int, 4>{}); break;
+        case 5: copy_cells(std::integral_constant<int, 5>{}); break;
+        case 6: copy_cells(std::integral_constant<int, 6>{}); break;
+        case 7: copy_cells(std::integral_constant<int, 7>{}); break;
+        case 8: copy_cells(std::integral_constant<int, 8>{}); break;
+        case 9: copy_cells(std::integral_constant<int, 9>{}); break;
+        case 10: copy_cells(std::integral_constant<int, 10>{}); break;
+        case 11: copy_cells(std::integral_constant<int, 11>{}); break;
+        case 12: copy_cells(std::integral_constant<int, 12>{}); break;
+        case 13: copy_cells(std::integral_constant<int, 13>{}); break;
+        case 14: copy_cells(std::integral_constant<int, 14>{}); break;
+        case 15: copy_cells(std::integral_constant<int, 15>{}); break;
+        case 16: copy_cells(std::integral_constant<int, 16>{}); break;
+        default: copy_cells(std::integral_constant<int, NC>{}); break;
       }
     } else {
       // one field: four cells' loads in flight per thread

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "vlct_physics.cuh"
+#include "vlct_types.h"
 
 namespace vlct {
 
@@ -72,6 +73,18 @@ template <class R> struct EnergyConsts {
     inv_gm1 = R(1. / (gamma - 1.));
     ggm1 = (float)(gamma * (gamma - 1.));
     pfloor = R(pressure_floor);
+    eta = R(eta_);
+    half_factor = (eta_ != 0.) ? R(0.5) : R(0.);
+  }
+  // the same values from the host-derived constants of the physics
+  // parameters, without the FP64 division: for kernels whose threads are
+  // short-lived (the timestep), where it would be a noticeable share
+  __host__ __device__ void init(const PhysParams& ph, bool de) {
+    gm1 = R(ph.gm1);
+    inv_gm1 = R(ph.inv_gm1);
+    ggm1 = (float)ph.ggm1;
+    pfloor = R(ph.pressure_floor);
+    const double eta_ = de ? ph.eta : 0.0;
     eta = R(eta_);
     half_factor = (eta_ != 0.) ? R(0.5) : R(0.);
   }

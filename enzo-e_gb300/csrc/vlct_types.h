@@ -54,6 +54,14 @@ struct PhysParams {
   double pressure_floor;
   double theta_limiter;
   double eta;
+  // derived on the host (set_derived), so that no kernel thread spends FP64
+  // divisions on them: gamma - 1, 1 / (gamma - 1), gamma (gamma - 1)
+  double gm1 = 0.0, inv_gm1 = 0.0, ggm1 = 0.0;
+  void set_derived() {
+    gm1 = gamma - 1.0;
+    inv_gm1 = 1. / (gamma - 1.);
+    ggm1 = gamma * (gamma - 1.);
+  }
 };
 
 // Per-stage scalars.
