@@ -316,123 +316,147 @@ __device__ __forceinline__ void hlld(R g, const R* wli, const R* wri,
   }
 }
 
-// HLLD in FP32: the same states and flux with shared denominators taken
-// once (one reciprocal per denominator, rsqrt for 1/sqrt(rho*)), and the
-// flux selected by its jump coefficients instead of forming every jump.
+// HLLD in FP32 (EnzoRiemannHLLD.hpp:40-448): the same states, wave speeds
+// and flux as the FP64 form, with fewer instructions.  The left and right
+// states ride in the two lanes of packed FP32 arithmetic (float2: fadd2 /
+// fmul2 / ffma2 on sm_100+), so every side-wise operation is one
+// instruction for both sides; each shared denominator is inverted once
+// (rsqrt for 1/sqrt(rho*)); the flux is F_side + c1 (U* - U) + c2 (U** - U*)
+// with the coefficients chosen in the reference's case order.  Differences
+// from the FP64 form lie only in rounding.
+namespace packed {
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 s2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b as one fused operation: b * -1 + a is exact before its one rounding
+__device__ __forceinline__ float2 sub(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+}  // namespace packed
+
 template <>
 __device__ __forceinline__ void hlld<float>(float g, const float* wli, const float* wri,
                                             FaceFlux<float>& out) {
+  using namespace packed;
   const float SMALL = 1.0e-8f;
   const float igm1 = 1.0f / (g - 1.0f);
-  const float pl = wli[L_E], pr = wri[L_E];
   const float bxi = wli[L_BI], bxsq = bxi * bxi;
-  const float dl = wli[L_RHO], dr = wri[L_RHO];
-  const float ul = wli[L_VI], ur = wri[L_VI];
-  const float inv_dl = 1.0f / dl, inv_dr = 1.0f / dr;
-  const float btl = wli[L_BJ] * wli[L_BJ] + wli[L_BK] * wli[L_BK];
-  const float btr = wri[L_BJ] * wri[L_BJ] + wri[L_BK] * wri[L_BK];
-  const float pbl = 0.5f * (bxsq + btl), pbr = 0.5f * (bxsq + btr);
-  const float kel = 0.5f * dl * (ul * ul + (wli[L_VJ] * wli[L_VJ] + wli[L_VK] * wli[L_VK]));
-  const float ker = 0.5f * dr * (ur * ur + (wri[L_VJ] * wri[L_VJ] + wri[L_VK] * wri[L_VK]));
-  const float ule = pl * igm1 + kel + pbl, ure = pr * igm1 + ker + pbr;
+  const float2 BXSQ = s2(bxsq), BXI = s2(bxi), HALF = s2(0.5f);
+  const float2 p = f2(wli[L_E], wri[L_E]);
+  const float2 d = f2(wli[L_RHO], wri[L_RHO]);
+  const float2 u = f2(wli[L_VI], wri[L_VI]);
+  const float2 vj = f2(wli[L_VJ], wri[L_VJ]), vk = f2(wli[L_VK], wri[L_VK]);
+  const float2 by = f2(wli[L_BJ], wri[L_BJ]), bz = f2(wli[L_BK], wri[L_BK]);
+  const float2 inv_d = f2(1.0f / d.x, 1.0f / d.y);
+  const float2 bt = fma(by, by, mul(bz, bz));
+  const float2 b2 = add(BXSQ, bt);
+  const float2 pb = mul(HALF, b2);
+  const float2 ke = mul(mul(HALF, d), fma(u, u, fma(vj, vj, mul(vk, vk))));
+  const float2 ue = add(fma(p, s2(igm1), ke), pb);
   // fast speeds (EnzoEOSIdeal.hpp:133-139)
-  auto cf = [&](float p, float inv_d, float bt) {
-    const float c2 = g * p * inv_d, va2 = (bxsq + bt) * inv_d, vac2 = bxsq * inv_d;
-    const float q = c2 + va2;
-    return sqrtf(0.5f * (va2 + c2 + sqrtf(q * q - 4.f * c2 * vac2)));
-  };
-  const float cfl = cf(pl, inv_dl, btl), cfr = cf(pr, inv_dr, btr);
-  const float spd0 = fminf(ul - cfl, ur - cfr);
-  const float spd4 = fmaxf(ul + cfl, ur + cfr);
-  const float ptl = pl + pbl, ptr = pr + pbr;
-  // left / right fluxes: d, mx, my, mz, e, by, bz
-  const float ulby = wli[L_BJ], ulbz = wli[L_BK], urby = wri[L_BJ], urbz = wri[L_BK];
-  const float FL[7] = {dl * ul, dl * ul * ul + ptl - bxsq, dl * wli[L_VJ] * ul - bxi * ulby,
-                       dl * wli[L_VK] * ul - bxi * ulbz,
-                       ul * (ule + ptl - bxsq) - bxi * (wli[L_VJ] * ulby + wli[L_VK] * ulbz),
-                       ulby * ul - bxi * wli[L_VJ], ulbz * ul - bxi * wli[L_VK]};
-  const float FR[7] = {dr * ur, dr * ur * ur + ptr - bxsq, dr * wri[L_VJ] * ur - bxi * urby,
-                       dr * wri[L_VK] * ur - bxi * urbz,
-                       ur * (ure + ptr - bxsq) - bxi * (wri[L_VJ] * urby + wri[L_VK] * urbz),
-                       urby * ur - bxi * wri[L_VJ], urbz * ur - bxi * wri[L_VK]};
-  const float sdl = spd0 - ul, sdr = spd4 - ur;
-  const float spd2 = (sdr * dr * ur - sdl * dl * ul + (ptl - ptr)) / (sdr * dr - sdl * dl);
-  const float sdml = spd0 - spd2, sdmr = spd4 - spd2;
-  const float lst_d = dl * sdl / sdml, rst_d = dr * sdr / sdmr;
-  const float isql = rsqrtf(lst_d), isqr = rsqrtf(rst_d);
-  const float sqrtdl = lst_d * isql, sqrtdr = rst_d * isqr;
-  const float lst_d_inv = isql * isql, rst_d_inv = isqr * isqr;
-  const float spd1 = spd2 - fabsf(bxi) * isql;
-  const float spd3 = spd2 + fabsf(bxi) * isqr;
-  const float ptst = 0.5f * ((ptr + dr * sdr * (spd2 - ur)) + (ptl + dl * sdl * (spd2 - ul)));
-  // single-star states: d, mx, my, mz, e, by, bz
-  float Ls[7], Rs[7];
-  auto star = [&](const float* w, float d, float sd, float sdm, float st_d, float st_d_inv,
-                  float by, float bz, float ue, float pt, float* S) {
-    S[0] = st_d;
-    S[1] = st_d * spd2;
-    const float den = d * sd * sdm - bxsq;
-    if (fabsf(den) < SMALL * ptst) {
-      S[2] = st_d * w[L_VJ]; S[3] = st_d * w[L_VK]; S[5] = by; S[6] = bz;
-    } else {
-      const float iden = 1.0f / den;
-      const float t1 = bxi * (sd - sdm) * iden;
-      S[2] = st_d * (w[L_VJ] - by * t1);
-      S[3] = st_d * (w[L_VK] - bz * t1);
-      const float t2 = (d * (sd * sd) - bxsq) * iden;
-      S[5] = by * t2; S[6] = bz * t2;
-    }
-    const float vbst = (S[1] * bxi + (S[2] * S[5] + S[3] * S[6])) * st_d_inv;
-    S[4] = (sd * ue - pt * w[L_VI] + ptst * spd2 +
-            bxi * (w[L_VI] * bxi + (w[L_VJ] * by + w[L_VK] * bz) - vbst)) / sdm;
-    return vbst;
-  };
-  const float vbstl = star(wli, dl, sdl, sdml, lst_d, lst_d_inv, ulby, ulbz, ule, ptl, Ls);
-  const float vbstr = star(wri, dr, sdr, sdmr, rst_d, rst_d_inv, urby, urbz, ure, ptr, Rs);
+  const float2 c2 = mul(mul(s2(g), p), inv_d);
+  const float2 va2 = mul(b2, inv_d);
+  const float2 vac2 = mul(BXSQ, inv_d);
+  const float2 q = add(c2, va2);
+  const float2 disc = fma(q, q, mul(mul(s2(-4.0f), c2), vac2));
+  const float2 inner = add(q, f2(sqrtf(disc.x), sqrtf(disc.y)));
+  const float2 cfh = mul(HALF, inner);
+  const float2 cf = f2(sqrtf(cfh.x), sqrtf(cfh.y));
+  const float2 um = sub(u, cf), up = add(u, cf);
+  const float spd0 = fminf(um.x, um.y);
+  const float spd4 = fmaxf(up.x, up.y);
+  const float2 pt = add(p, pb);
+  // side fluxes: d, mx, my, mz, e, by, bz
+  const float2 du = mul(d, u);
+  const float2 vbt = fma(vj, by, mul(vk, bz));
+  const float2 ptb = sub(pt, BXSQ);
+  const float2 F[7] = {du, fma(du, u, ptb), sub(mul(du, vj), mul(BXI, by)),
+                       sub(mul(du, vk), mul(BXI, bz)), sub(mul(u, add(ue, ptb)), mul(BXI, vbt)),
+                       sub(mul(by, u), mul(BXI, vj)), sub(mul(bz, u), mul(BXI, vk))};
+  const float2 S04 = f2(spd0, spd4);
+  const float2 sd = sub(S04, u);
+  const float2 sdd = mul(sd, d);
+  const float2 sddu = mul(sdd, u);
+  const float spd2 = (sddu.y - sddu.x + (pt.x - pt.y)) / (sdd.y - sdd.x);
+  const float2 SPD2 = s2(spd2);
+  const float2 sdm = sub(S04, SPD2);
+  const float2 st_d = f2(sdd.x / sdm.x, sdd.y / sdm.y);
+  const float2 isq = f2(rsqrtf(st_d.x), rsqrtf(st_d.y));
+  const float2 sqrtd = mul(st_d, isq);
+  const float2 st_d_inv = mul(isq, isq);
+  const float spd1 = spd2 - fabsf(bxi) * isq.x;
+  const float spd3 = spd2 + fabsf(bxi) * isq.y;
+  const float2 ptw = fma(sdd, sub(SPD2, u), pt);
+  const float ptst = 0.5f * (ptw.y + ptw.x);
+  // single-star states, both sides at once: d, mx, my, mz, e, by, bz; a
+  // side whose |d s (s - s_M) - B_x^2| is below SMALL p* keeps its
+  // transverse B and velocity (t1 = 0, t2 = 1)
+  const float2 den = sub(mul(sdd, sdm), BXSQ);
+  const float thr = SMALL * ptst;
+  const bool degl = fabsf(den.x) < thr, degr = fabsf(den.y) < thr;
+  const float2 iden = f2(1.0f / den.x, 1.0f / den.y);
+  float2 t1 = mul(mul(BXI, sub(sd, sdm)), iden);
+  float2 t2 = mul(sub(mul(sdd, sd), BXSQ), iden);
+  t1 = f2(degl ? 0.0f : t1.x, degr ? 0.0f : t1.y);
+  t2 = f2(degl ? 1.0f : t2.x, degr ? 1.0f : t2.y);
+  float2 Us[7];
+  Us[0] = st_d;
+  Us[1] = mul(st_d, SPD2);
+  Us[2] = mul(st_d, sub(vj, mul(by, t1)));
+  Us[3] = mul(st_d, sub(vk, mul(bz, t1)));
+  Us[5] = mul(by, t2);
+  Us[6] = mul(bz, t2);
+  const float2 vbst = mul(fma(Us[1], BXI, fma(Us[2], Us[5], mul(Us[3], Us[6]))), st_d_inv);
+  const float2 e_num =
+      add(fma(SPD2, s2(ptst), sub(mul(sd, ue), mul(pt, u))), mul(BXI, sub(fma(u, BXI, vbt), vbst)));
+  Us[4] = f2(e_num.x / sdm.x, e_num.y / sdm.y);
   // double-star states
-  float Ld[7], Rd[7];
+  float2 Ud[7];
 #pragma unroll
-  for (int k = 0; k < 7; k++) { Ld[k] = Ls[k]; Rd[k] = Rs[k]; }
+  for (int k = 0; k < 7; k++) Ud[k] = Us[k];
   if (!(0.5f * bxsq < SMALL * ptst)) {
-    const float invsumd = 1.0f / (sqrtdl + sqrtdr);
+    const float invsumd = 1.0f / (sqrtd.x + sqrtd.y);
     const float bxsig = bxi > 0.0f ? 1.0f : -1.0f;
-    const float vyl = Ls[2] * lst_d_inv, vyr = Rs[2] * rst_d_inv;
-    const float vzl = Ls[3] * lst_d_inv, vzr = Rs[3] * rst_d_inv;
-    const float ty = invsumd * (sqrtdl * vyl + sqrtdr * vyr + bxsig * (Rs[5] - Ls[5]));
-    const float tz = invsumd * (sqrtdl * vzl + sqrtdr * vzr + bxsig * (Rs[6] - Ls[6]));
-    Ld[2] = Ls[0] * ty; Rd[2] = Rs[0] * ty;
-    Ld[3] = Ls[0] * tz; Rd[3] = Rs[0] * tz;
-    const float sq = bxsig * sqrtdl * sqrtdr;
-    const float by = invsumd * (sqrtdl * Rs[5] + sqrtdr * Ls[5] + sq * (vyr - vyl));
-    const float bz = invsumd * (sqrtdl * Rs[6] + sqrtdr * Ls[6] + sq * (vzr - vzl));
-    Ld[5] = Rd[5] = by; Ld[6] = Rd[6] = bz;
-    const float t = spd2 * bxi + (Ld[2] * by + Ld[3] * bz) * lst_d_inv;
-    Ld[4] = Ls[4] - sqrtdl * bxsig * (vbstl - t);
-    Rd[4] = Rs[4] + sqrtdr * bxsig * (vbstr - t);
+    const float2 vy = mul(Us[2], st_d_inv), vz = mul(Us[3], st_d_inv);
+    const float2 wvy = mul(sqrtd, vy), wvz = mul(sqrtd, vz);
+    const float ty = invsumd * (wvy.x + wvy.y + bxsig * (Us[5].y - Us[5].x));
+    const float tz = invsumd * (wvz.x + wvz.y + bxsig * (Us[6].y - Us[6].x));
+    Ud[2] = mul(Us[0], s2(ty));
+    Ud[3] = mul(Us[0], s2(tz));
+    const float sq = bxsig * sqrtd.x * sqrtd.y;
+    const float byd = invsumd * (sqrtd.x * Us[5].y + sqrtd.y * Us[5].x + sq * (vy.y - vy.x));
+    const float bzd = invsumd * (sqrtd.x * Us[6].y + sqrtd.y * Us[6].x + sq * (vz.y - vz.x));
+    Ud[5] = s2(byd);
+    Ud[6] = s2(bzd);
+    // v** . B** from the left side's values for both (as the scalar form)
+    const float tl = spd2 * bxi + (Ud[2].x * byd + Ud[3].x * bzd) * st_d_inv.x;
+    const float2 sg = mul(sqrtd, f2(-bxsig, bxsig));
+    Ud[4] = fma(sg, sub(vbst, s2(tl)), Us[4]);
   }
   // F = F_side + c1 (U* - U) + c2 (U** - U*), the cases in the reference's
   // order: F_L (spd0 >= 0), F_R (spd4 <= 0), then by the signs of spd1..spd3
   const bool outer = spd0 >= 0.0f || spd4 <= 0.0f;
   const bool left = spd0 >= 0.0f || (!(spd4 <= 0.0f) && spd2 >= 0.0f);
   const float c1 = outer ? 0.0f : (left ? spd0 : spd4);
-  const float c2 = outer ? 0.0f : (left ? (spd1 >= 0.0f ? 0.0f : spd1)
-                                        : (spd3 > 0.0f ? spd3 : 0.0f));
-  const float U0[7] = {dl, dl * ul, dl * wli[L_VJ], dl * wli[L_VK], ule, ulby, ulbz};
-  const float U1[7] = {dr, dr * ur, dr * wri[L_VJ], dr * wri[L_VK], ure, urby, urbz};
+  const float c2v = outer ? 0.0f : (left ? (spd1 >= 0.0f ? 0.0f : spd1)
+                                         : (spd3 > 0.0f ? spd3 : 0.0f));
+  const float2 U[7] = {d, du, mul(d, vj), mul(d, vk), ue, by, bz};
   float Fo[7];
 #pragma unroll
   for (int k = 0; k < 7; k++) {
-    const float F = left ? FL[k] : FR[k], U = left ? U0[k] : U1[k];
-    const float Us = left ? Ls[k] : Rs[k], Ud = left ? Ld[k] : Rd[k];
-    Fo[k] = F + c1 * (Us - U) + c2 * (Ud - Us);
+    const float Fk = left ? F[k].x : F[k].y, Uk = left ? U[k].x : U[k].y;
+    const float Usk = left ? Us[k].x : Us[k].y, Udk = left ? Ud[k].x : Ud[k].y;
+    Fo[k] = Fk + c1 * (Usk - Uk) + c2v * (Udk - Usk);
   }
   out.f[L_RHO] = Fo[0]; out.f[L_VI] = Fo[1]; out.f[L_VJ] = Fo[2]; out.f[L_VK] = Fo[3];
   out.f[L_E] = Fo[4]; out.f[L_BJ] = Fo[5]; out.f[L_BK] = Fo[6];
   out.f[L_BI] = 0.0f;
-  out.eflux = eint_flux(g, dl, pl, dr, pr, out.f[L_RHO]);
-  if (spd0 > 0.0f) out.vbar = ul;
-  else if (spd4 < 0.0f) out.vbar = ur;
-  else out.vbar = spd2 * (spd2 >= 0.0f ? sdl / sdml : sdr / sdmr);
+  out.eflux = eint_flux(g, d.x, p.x, d.y, p.y, out.f[L_RHO]);
+  if (spd0 > 0.0f) out.vbar = u.x;
+  else if (spd4 < 0.0f) out.vbar = u.y;
+  else out.vbar = spd2 * (spd2 >= 0.0f ? sd.x / sdm.x : sd.y / sdm.y);
 }
 
 // conserved state from primitives (EnzoRiemannUtils.hpp:48-82)
