@@ -334,122 +334,158 @@ refresh_shell_kernel(const AuxBlock<R>* __restrict__ blocks, const int* __restri
   auto mdiv = [](int v, unsigned d, unsigned m) -> int {
     return d > 1 ? (int)__umulhi((unsigned)v, m) : v;
   };
-  // face = -1: the cell-centred shell (all cell fields); 0..2: the shell of
-  // bfieldi along that axis
-  for (int face = -1; face < 3; face++) {
-    if (face >= 0 && !s_fdst[face]) continue;
-    int e[3], hi[3];
-    for (int a = 0; a < 3; a++) {
-      e[a] = B.m[a] + (a == face);
-      hi[a] = (a == face) ? g + n[a] + 1 : g + n[a];
-    }
-    const int wz = e[2] - (hi[2] - g), wy = e[1] - (hi[1] - g), wx = e[0] - (hi[0] - g);
-    const int iz = hi[2] - g, iy = hi[1] - g;
-    const unsigned m0 = magic(e[0]), m1 = magic(e[1]), mwy = magic(wy), mwx = magic(wx),
-                   miy = magic(iy);
-    const int cz = wz * e[1] * e[0];
-    const int cy = iz * wy * e[0];
-    const int cx = iz * iy * wx;
-    const int total = cz + cy + cx;
-    // the destination and source index of shell cell q (and the source's
-    // neighbour slot k)
-    auto locate = [&](int q, size_t& di, size_t& si, int& k) {
-      int x, y, z;
+  // Pass 1: the cell shell -- z-slabs, then y-slabs, then the x-ends.  Each
+  // ghost cell copies every cell field and, with face-centred B, the face
+  // values on its low side along each axis (bfieldi_a at the cell's index),
+  // so one position decode serves up to 12 fields.  Face index g + n along
+  // its own axis is the block's own boundary face: along that axis it sits
+  // "inside" (neighbour offset 0), and it is skipped when it is inside along
+  // every axis.  Pass 2 covers the face layers above the last cell
+  // (bfieldi_a at index m along a).
+  const int M[3] = {B.m[0], B.m[1], B.m[2]};
+  const int HI[3] = {g + n[0], g + n[1], g + n[2]};
+  const int wz = M[2] - n[2], wy = M[1] - n[1], wx = M[0] - n[0];
+  const int iz = n[2], iy = n[1];
+  const unsigned m0 = magic(M[0]), m1 = magic(M[1]), mwy = magic(wy), mwx = magic(wx),
+                 miy = magic(iy);
+  const int cz = wz * M[1] * M[0];
+  const int cy = iz * wy * M[0];
+  const int cx = iz * iy * wx;
+  const int total = cz + cy + cx;
+  const int stride = chunks_per_block * blockDim.x;
+  const bool faces = s_fdst[0] != nullptr;  // MHD: all three, or none
+  auto side_of = [&](int a, int i) { return (i < g) ? -1 : ((i >= HI[a]) ? 1 : 0); };
+  auto slot_of = [](const int* sd) { return (sd[2] + 1) * 9 + (sd[1] + 1) * 3 + (sd[0] + 1); };
+  // index of (x, y, z) in the face array of axis a
+  auto face_index = [&](int a, const int* i) -> size_t {
+    const int e0 = M[0] + (a == 0), e1 = M[1] + (a == 1);
+    return ((size_t)i[2] * e1 + i[1]) * e0 + i[0];
+  };
+  auto copy_shell = [&](auto count, auto with_faces) {
+    constexpr int N = decltype(count)::value;
+    constexpr bool F = decltype(with_faces)::value;
+    for (int q = chunk * blockDim.x + threadIdx.x; q < total; q += stride) {
+      int idx[3];
       if (q < cz) {
-        const int r1 = mdiv(q, e[0], m0);
-        x = q - r1 * e[0];
-        const int r2 = mdiv(r1, e[1], m1);
-        y = r1 - r2 * e[1];
-        z = (r2 < g) ? r2 : r2 + iz;
+        const int r1 = mdiv(q, M[0], m0);
+        idx[0] = q - r1 * M[0];
+        const int r2 = mdiv(r1, M[1], m1);
+        idx[1] = r1 - r2 * M[1];
+        idx[2] = (r2 < g) ? r2 : r2 + iz;
       } else if (q < cz + cy) {
         const int r0 = q - cz;
-        const int r1 = mdiv(r0, e[0], m0);
-        x = r0 - r1 * e[0];
+        const int r1 = mdiv(r0, M[0], m0);
+        idx[0] = r0 - r1 * M[0];
         const int r2 = mdiv(r1, wy, mwy);
         const int yy = r1 - r2 * wy;
-        y = (yy < g) ? yy : yy + iy;
-        z = g + r2;
+        idx[1] = (yy < g) ? yy : yy + iy;
+        idx[2] = g + r2;
       } else {
         const int r0 = q - cz - cy;
         const int r1 = mdiv(r0, wx, mwx);
         const int xx = r0 - r1 * wx;
-        x = (xx < g) ? xx : xx + (hi[0] - g);
+        idx[0] = (xx < g) ? xx : xx + n[0];
         const int r2 = mdiv(r1, iy, miy);
-        y = g + (r1 - r2 * iy);
-        z = g + r2;
+        idx[1] = g + (r1 - r2 * iy);
+        idx[2] = g + r2;
       }
-      // source index and neighbour offset per axis; a face axis keeps the
-      // block's own boundary faces (k = g, g + n)
       int side[3], src[3];
-      const int idx[3] = {x, y, z};
 #pragma unroll
       for (int a = 0; a < 3; a++) {
-        const int i = idx[a];
-        side[a] = (i < g) ? -1 : ((i >= hi[a]) ? 1 : 0);
-        src[a] = i - side[a] * n[a];
+        side[a] = side_of(a, idx[a]);
+        src[a] = idx[a] - side[a] * n[a];
       }
-      k = (side[2] + 1) * 9 + (side[1] + 1) * 3 + (side[0] + 1);
-      di = ((size_t)z * e[1] + y) * e[0] + x;
-      si = ((size_t)src[2] * e[1] + src[1]) * e[0] + src[0];
-    };
-    const int stride = chunks_per_block * blockDim.x;
-    if (face < 0) {
-      // every field of a cell: all loads issued before any store (through
-      // the pointer tables the compiler cannot rule out aliasing, and would
-      // otherwise wait out one memory round trip per field); the loop is
-      // compiled for the block's exact field count
-      auto copy_cells = [&](auto count) {
-        constexpr int N = decltype(count)::value;
-        for (int q = chunk * blockDim.x + threadIdx.x; q < total; q += stride) {
-          size_t di, si;
-          int k;
-          locate(q, di, si, k);
-          R v[N];
+      const int k = slot_of(side);
+      const size_t di = ((size_t)idx[2] * M[1] + idx[1]) * M[0] + idx[0];
+      const size_t si = ((size_t)src[2] * M[1] + src[1]) * M[0] + src[0];
+      // all loads of the cell before any store (through the pointer tables
+      // the compiler cannot rule out aliasing, and would otherwise wait out
+      // one memory round trip per field)
+      R v[N];
 #pragma unroll
-          for (int j = 0; j < N; j++) v[j] = s_src[j][k][si];
+      for (int j = 0; j < N; j++) v[j] = s_src[j][k][si];
+      R fv[3];
+      size_t fdi[3];
+      bool fon[3] = {false, false, false};
+      if (F) {
 #pragma unroll
-          for (int j = 0; j < N; j++) s_dst[j][di] = v[j];
+        for (int a = 0; a < 3; a++) {
+          int fs[3] = {side[0], side[1], side[2]};
+          if (idx[a] == HI[a]) fs[a] = 0;  // the face at g + n along a
+          if (fs[0] == 0 && fs[1] == 0 && fs[2] == 0) continue;
+          const int fsrc[3] = {idx[0] - fs[0] * n[0], idx[1] - fs[1] * n[1],
+                               idx[2] - fs[2] * n[2]};
+          fon[a] = true;
+          fdi[a] = face_index(a, idx);
+          fv[a] = s_fsrc[a][slot_of(fs)][face_index(a, fsrc)];
         }
-      };
-      switch (nc) {
-        case 1: copy_cells(std::integral_constant<int, 1>{}); break;
-        case 2: copy_cells(std::integral_constant<int, 2>{}); break;
-        case 3: copy_cells(std::integral_constant<int, 3>{}); break;
-        case 4: copy_cells(std::integral_constant<int, 4>{}); break;
-        case 5: copy_cells(std::integral_constant<int, 5>{}); break;
-        case 6: copy_cells(std::integral_constant<int, 6>{}); break;
-        case 7: copy_cells(std::integral_constant<int, 7>{}); break;
-        case 8: copy_cells(std::integral_constant<int, 8>{}); break;
-        case 9: copy_cells(std::integral_constant<int, 9>{}); break;
-        case 10: copy_cells(std::integral_constant<int, 10>{}); break;
-        case 11: copy_cells(std::integral_constant<int, 11>{}); break;
-        case 12: copy_cells(std::integral_constant<int, 12>{}); break;
-        case 13: copy_cells(std::integral_constant<int, 13>{}); break;
-        case 14: copy_cells(std::integral_constant<int, 14>{}); break;
-        case 15: copy_cells(std::integral_constant<int, 15>{}); break;
-        case 16: copy_cells(std::integral_constant<int, 16>{}); break;
-        default: copy_cells(std::integral_constant<int, NC>{}); break;
       }
-    } else {
-      // one field: four cells' loads in flight per thread
-      constexpr int U = 4;
-      for (int q0 = chunk * blockDim.x + threadIdx.x; q0 < total; q0 += U * stride) {
-        size_t di[U];
-        R v[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-          const int q = q0 + u * stride;
-          if (q < total) {
-            size_t si;
-            int k;
-            locate(q, di[u], si, k);
-            v[u] = s_fsrc[face][k][si];
-          }
-        }
+      for (int j = 0; j < N; j++) s_dst[j][di] = v[j];
+      if (F) {
 #pragma unroll
-        for (int u = 0; u < U; u++)
-          if (q0 + u * stride < total) s_fdst[face][di[u]] = v[u];
+        for (int a = 0; a < 3; a++)
+          if (fon[a]) s_fdst[a][fdi[a]] = fv[a];
       }
+    }
+  };
+  auto dispatch = [&](auto with_faces) {
+    switch (nc) {
+      case 1: copy_shell(std::integral_constant<int, 1>{}, with_faces); break;
+      case 2: copy_shell(std::integral_constant<int, 2>{}, with_faces); break;
+      case 3: copy_shell(std::integral_constant<int, 3>{}, with_faces); break;
+      case 4: copy_shell(std::integral_constant<int, 4>{}, with_faces); break;
+      case 5: copy_shell(std::integral_constant<int, 5>{}, with_faces); break;
+      case 6: copy_shell(std::integral_constant<int, 6>{}, with_faces); break;
+      case 7: copy_shell(std::integral_constant<int, 7>{}, with_faces); break;
+      case 8: copy_shell(std::integral_constant<int, 8>{}, with_faces); break;
+      case 9: copy_shell(std::integral_constant<int, 9>{}, with_faces); break;
+      case 10: copy_shell(std::integral_constant<int, 10>{}, with_faces); break;
+      case 11: copy_shell(std::integral_constant<int, 11>{}, with_faces); break;
+      case 12: copy_shell(std::integral_constant<int, 12>{}, with_faces); break;
+      case 13: copy_shell(std::integral_constant<int, 13>{}, with_faces); break;
+      case 14: copy_shell(std::integral_constant<int, 14>{}, with_faces); break;
+      case 15: copy_shell(std::integral_constant<int, 15>{}, with_faces); break;
+      case 16: copy_shell(std::integral_constant<int, 16>{}, with_faces); break;
+      default: copy_shell(std::integral_constant<int, NC>{}, with_faces); break;
+    }
+  };
+  if (faces)
+    dispatch(std::integral_constant<bool, true>{});
+  else
+    dispatch(std::integral_constant<bool, false>{});
+  if (!faces) return;
+  // Pass 2: bfieldi_a at index m along a (above the last cell), every
+  // position across; neighbour offset +1 along a
+  for (int a = 0; a < 3; a++) {
+    const int b0 = a == 0 ? 1 : 0, b1 = a == 2 ? 1 : 2;  // the other axes, inner first
+    const int layer = M[b0] * M[b1];
+    const unsigned mb = magic(M[b0]);
+    constexpr int U = 4;
+    for (int q0 = chunk * blockDim.x + threadIdx.x; q0 < layer; q0 += U * stride) {
+      size_t fdi[U];
+      R fv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int q = q0 + u * stride;
+        if (q >= layer) continue;
+        const int r = mdiv(q, M[b0], mb);
+        int idx[3];
+        idx[a] = M[a];
+        idx[b0] = q - r * M[b0];
+        idx[b1] = r;
+        int fs[3];
+        fs[a] = 1;
+        fs[b0] = side_of(b0, idx[b0]);
+        fs[b1] = side_of(b1, idx[b1]);
+        const int fsrc[3] = {idx[0] - fs[0] * n[0], idx[1] - fs[1] * n[1],
+                             idx[2] - fs[2] * n[2]};
+        fdi[u] = face_index(a, idx);
+        fv[u] = s_fsrc[a][slot_of(fs)][face_index(a, fsrc)];
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (q0 + u * stride < layer) s_fdst[a][fdi[u]] = fv[u];
     }
   }
 }
