@@ -1,7 +1,8 @@
-"""Passive scalars through the C ABI: the CUDA step equals the oracle (pinned
-bit for bit to the reference in tests/test_passive_oracle.py) in FP64 and
-stays within 1e-5 relative L1 in FP32; the periodic ghost refresh covers the
-scalar fields; the no-alloc entry point refuses them."""
+"""Passive scalars through the C ABI (the stage kernel writes the density
+fluxes, passive_kernel advects the scalars): the CUDA step equals the oracle
+(pinned bit for bit to the reference in tests/test_passive_oracle.py) in FP64
+and stays within 1e-5 relative L1 in FP32; the periodic ghost refresh covers
+the scalar fields; the no-alloc entry point equals the oracle too."""
 import ctypes
 
 import numpy as np
