@@ -184,12 +184,22 @@ TileChoice choice_for(const mhdvlct_batch* b, int i) {
       return n;
     }();
     const int target = 4 * nsm;
-    for (int s = 0; s < 2; s++) {
+    auto columns_of = [&](int tx, int ty) {
       long columns = 0;
       for (int k = 0; k < b->nblocks; k++) {
         const int mx = b->dims[3 * k] + 2 * b->g, my = b->dims[3 * k + 1] + 2 * b->g;
-        columns += (long)((mx + c.tile_x[s] - 1) / c.tile_x[s]) *
-                   ((my + c.tile_y[s] - 1) / c.tile_y[s]);
+        columns += (long)((mx + tx - 1) / tx) * ((my + ty - 1) / ty);
+      }
+      return columns;
+    };
+    for (int s = 0; s < 2; s++) {
+      long columns = columns_of(c.tile_x[s], c.tile_y[s]);
+      if (columns < target && c.tile_x[s] != c.tile_y[s]) {
+        // a batch too small to fill the GPU with the large rectangular
+        // tiles: the smaller square tile (several CTAs per SM) instead
+        const int t = default_tile(b->dtype, b->h->solver, sp.recon[s], b->h->de);
+        c.tile_x[s] = c.tile_y[s] = t;
+        columns = columns_of(t, t);
       }
       const int mz = b->dims[3 * i + 2] + 2 * b->g;
       if (columns < target && mz > 24) {
