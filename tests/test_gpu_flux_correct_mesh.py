@@ -279,3 +279,51 @@ def test_batch_graph_passive_flux_correction_bit_exact():
         got = bt.download(i)
         for k, o in zip(NAMES + PNAMES, ONAMES + PONAMES):
             assert np.array_equal(got[k], ob.f[o]), (i, k)
+
+
+def test_fp32_passive_correction_bit_exact_with_conservative_scalar():
+    # the correction alone on random fields and fluxes, with two passive
+    # scalars in the group; scalar 1 is in the "make_field_conservative"
+    # mask (field bit MHD_FIELD_PASSIVE_0 + 1), so it is corrected as
+    # old density x value, divided by the corrected density
+    n, g = 8, 4
+    mesh = M.Mesh((2, 2, 2), refine=lambda lvl, c: c == (0, 0, 0))
+    rng = np.random.default_rng(37)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc")
+    qs = (0, 1, 2, 3, 4) + tuple(capi.MHD_Q_PASSIVE_0 + k for k in range(NPASS))
+    keys = NAMES + PNAMES
+    blocks, bufs, ofields, ofluxes = [], [], [], []
+    m = n + 2 * g
+    for _ in mesh.leaves:
+        st = {"density": 0.5 + rng.random((m, m, m))}
+        for k in keys[1:]:
+            st[k] = rng.standard_normal((m, m, m))
+        st = {k: v.astype(np.float32) for k, v in st.items()}
+        b = B.Block((n,) * 3, g, (1.0, 1.0, 1.0), mhd=False, dtype=torch.float32,
+                    npassive=NPASS)
+        b.load_numpy(st)
+        buf = B.FluxBuffers(b, qs)
+        fx = {}
+        for key, t in buf.arrays.items():
+            a = rng.standard_normal(tuple(t.shape)).astype(np.float32)
+            t.copy_(torch.from_numpy(a))
+            fx[key] = a
+        blocks.append(b)
+        bufs.append(buf)
+        of = {q: st[k].copy() for q, k in enumerate(NAMES)}
+        for k in range(NPASS):
+            of[capi.MHD_Q_PASSIVE_0 + k] = st[PNAMES[k]].copy()
+        ofields.append(of)
+        ofluxes.append(fx)
+    cons = capi.MHD_CONSERVATIVE_DEFAULT | (1 << (capi.MHD_FIELD_PASSIVE_0 + 1))
+    # the oracle takes the mask in its own slots (MHD_Q_*)
+    ocons = capi.MHD_CONSERVATIVE_DEFAULT | (1 << (capi.MHD_Q_PASSIVE_0 + 1))
+    meth.flux_correct(blocks, bufs, mesh.face_array(), cons)
+    torch.cuda.synchronize()
+    O.flux_correct(ofields, ofluxes, (n,) * 3, (g,) * 3, mesh.face_ints(), ocons)
+    for i, b in enumerate(blocks):
+        got = b.to_numpy()
+        for q, k in enumerate(NAMES):
+            assert np.array_equal(got[k], ofields[i][q]), (i, k)
+        for k in range(NPASS):
+            assert np.array_equal(got[PNAMES[k]], ofields[i][capi.MHD_Q_PASSIVE_0 + k]), (i, k)
