@@ -633,6 +633,82 @@ __device__ __forceinline__ void hllc(R g, const R* wl, const R* wr,
   out.vbar = (sl * (wl[L_VI] - bm) + sr * (wr[L_VI] - bp));
 }
 
+// HLLC in FP32 (EnzoRiemannHLLC.hpp:34-172 with the Einfeldt speeds of
+// EnzoRiemannHLL.hpp:44-172): the same states, speeds and flux as the FP64
+// form, the left and right states in the two lanes of packed FP32
+// arithmetic.  Differences from the FP64 form lie only in rounding.
+template <>
+__device__ __forceinline__ void hllc<float>(float g, const float* wl, const float* wr,
+                                            FaceFlux<float>& out) {
+  using namespace packed;
+  const float2 HALF = s2(0.5f);
+  const float2 p = f2(wl[L_E], wr[L_E]);
+  const float2 d = f2(wl[L_RHO], wr[L_RHO]);
+  const float2 u = f2(wl[L_VI], wr[L_VI]);
+  const float2 vj = f2(wl[L_VJ], wr[L_VJ]), vk = f2(wl[L_VK], wr[L_VK]);
+  const float2 inv_d = f2(1.0f / d.x, 1.0f / d.y);
+  const float gm1 = g - 1.0f;
+  // conserved momentum and total energy density
+  const float2 mom = mul(u, d);
+  const float2 v2 = fma(u, u, fma(vj, vj, mul(vk, vk)));
+  const float2 E = fma(p, s2(1.0f / gm1), mul(mul(HALF, d), v2));
+  // Einfeldt speeds: sound speeds, Roe averages
+  const float2 c2 = mul(mul(s2(g), p), inv_d);
+  const float left_speed = u.x - sqrtf(c2.x), right_speed = u.y + sqrtf(c2.y);
+  const float2 sq = f2(sqrtf(d.x), sqrtf(d.y));
+  const float inv_tot = 1.0f / (sq.x + sq.y);
+  const float2 su = mul(sq, u), sv = mul(sq, vj), sw = mul(sq, vk);
+  const float vi_roe = (su.x + su.y) * inv_tot;
+  const float vj_roe = (sv.x + sv.y) * inv_tot;
+  const float vk_roe = (sw.x + sw.y) * inv_tot;
+  const float v_roe2 = vi_roe * vi_roe + vj_roe * vj_roe + vk_roe * vk_roe;
+  const float2 sh = mul(sq, mul(add(E, p), inv_d));
+  const float h_roe = (sh.x + sh.y) * inv_tot;
+  const float c_roe = sqrtf(gm1 * smax(h_roe - 0.5f * v_roe2, 0.0f));
+  const float cs_r = fmaxf(vi_roe + c_roe, right_speed);
+  const float cs_l = fminf(vi_roe - c_roe, left_speed);
+  const float bm = fminf(cs_l, 0.0f);
+  const float bp = fmaxf(cs_r, 0.0f);
+  // contact speed and pressure
+  const float2 cu = sub(f2(cs_l, cs_r), u);
+  const float2 t = sub(p, mul(cu, mom));
+  const float2 dd = mul(d, cu);
+  const float dl = dd.x, dr = -dd.y;
+  const float q1 = 1.0f / (dl + dr);
+  const float cw = (t.y - t.x) * q1;
+  float cp = (dl * t.y + dr * t.x) * q1;
+  float sl, sr, sm;
+  if (cw >= 0.0f) {
+    sl = cw / (cw - bm);
+    sr = 0.0f;
+    sm = -bm / (cw - bm);
+  } else {
+    sl = 0.0f;
+    sr = -cw / (bp - cw);
+    sm = bp / (bp - cw);
+  }
+  cp = smax(cp, 0.0f);
+  // side fluxes relative to the outer wave speeds
+  const float2 B = f2(bm, bp);
+  const float2 ub = sub(u, B);
+  const float2 df = sub(mom, mul(B, d));
+  const float2 uf = fma(mom, ub, p);
+  const float2 vf = mul(mul(d, vj), ub);
+  const float2 wf = mul(mul(d, vk), ub);
+  const float2 ef = fma(E, ub, mul(p, u));
+  const float2 SLR = f2(sl, sr);
+  const float2 frho = mul(SLR, df), fu = mul(SLR, uf), fv = mul(SLR, vf), fw = mul(SLR, wf),
+               fe = mul(SLR, ef), fvb = mul(SLR, ub);
+  out.f[L_RHO] = frho.x + frho.y;
+  out.f[L_VI] = (fu.x + fu.y) + sm * cp;
+  out.f[L_VJ] = fv.x + fv.y;
+  out.f[L_VK] = fw.x + fw.y;
+  out.f[L_E] = (fe.x + fe.y) + sm * cp * cw;
+  out.f[L_BI] = out.f[L_BJ] = out.f[L_BK] = 0.0f;
+  out.eflux = eint_flux(g, d.x, p.x, d.y, p.y, out.f[L_RHO]);
+  out.vbar = fvb.x + fvb.y;
+}
+
 template <int SOLVER, class R>
 __device__ __forceinline__ void riemann(R g, const R* wl, const R* wr,
                                         FaceFlux<R>& out) {
