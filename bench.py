@@ -66,7 +66,7 @@ def _args():
                          "mixed-size block set, the serving stream, the FP32-vs-FP64 "
                          "study (one JSON line each)")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--smr-root", type=int, default=8,
                     help="smr mode: root blocks per axis (the central half is refined)")
     ap.add_argument("--no-smr", action="store_true",
@@ -493,7 +493,7 @@ def make_batch_general(meth, blocks, dims, widths, dtype, nbr, ghost=GHOST, npas
     return h
 
 
-def run_serve(seed=4, nreq=24, rate_hz=30.0, cycles=20, budget_gib=6.0,
+def run_serve(seed=4, nreq=48, rate_hz=30.0, cycles=20, budget_gib=6.0,
               max_active=32):
     """Serving stream (Poisson arrivals of independent solves): grids on
     {32,64,96,128}^3, solver on {hlle, hllc (hydro), hlld}, reconstruction on
@@ -513,7 +513,9 @@ def run_serve(seed=4, nreq=24, rate_hz=30.0, cycles=20, budget_gib=6.0,
         # a client holds its fields in the request's precision already
         state = {k: np.ascontiguousarray(v, dtype=np.float32) for k, v in state.items()}
         specs.append((n, solver, recon, state, box))
-    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, nreq))
+    # arrival times from a stream of their own, so that a shorter run is a
+    # prefix of a longer one (requests and arrivals alike)
+    arrivals = np.cumsum(np.random.default_rng(seed + 1).exponential(1.0 / rate_hz, nreq))
     srv = S.Server(int(budget_gib * 2 ** 30), max_active=max_active, courant=COURANT)
     # warm the server, untimed: every (solver, reconstruction) kernel once, and
     # a few requests of every grid size at once, so that its staging buffers
