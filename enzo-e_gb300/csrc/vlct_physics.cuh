@@ -633,6 +633,94 @@ __device__ __forceinline__ void hllc(R g, const R* wl, const R* wr,
   out.vbar = (sl * (wl[L_VI] - bm) + sr * (wr[L_VI] - bp));
 }
 
+// HLLE in FP32 (EnzoRiemannHLL.hpp:44-345): the same states, Einfeldt
+// speeds and flux as the FP64 form, the left and right states in the two
+// lanes of packed FP32 arithmetic.  Differences from the FP64 form lie only
+// in rounding.
+template <>
+__device__ __forceinline__ void hlle<float>(float g, const float* wl, const float* wr,
+                                            FaceFlux<float>& out) {
+  using namespace packed;
+  const float2 HALF = s2(0.5f);
+  const float2 p = f2(wl[L_E], wr[L_E]);
+  const float2 d = f2(wl[L_RHO], wr[L_RHO]);
+  const float2 u = f2(wl[L_VI], wr[L_VI]);
+  const float2 vj = f2(wl[L_VJ], wr[L_VJ]), vk = f2(wl[L_VK], wr[L_VK]);
+  const float2 bi = f2(wl[L_BI], wr[L_BI]);
+  const float2 bj = f2(wl[L_BJ], wr[L_BJ]), bk = f2(wl[L_BK], wr[L_BK]);
+  const float2 inv_d = f2(1.0f / d.x, 1.0f / d.y);
+  const float gm1 = g - 1.0f;
+  // conserved states and physical fluxes (EnzoRiemannUtils.hpp:48-149)
+  const float2 mi = mul(u, d), mj = mul(vj, d), mk = mul(vk, d);
+  const float2 b2 = fma(bi, bi, fma(bj, bj, mul(bk, bk)));
+  const float2 v2 = fma(u, u, fma(vj, vj, mul(vk, vk)));
+  const float2 E = add(fma(p, s2(1.0f / gm1), mul(mul(HALF, d), v2)), mul(HALF, b2));
+  const float2 pt = fma(HALF, b2, p);
+  const float2 vb = fma(bi, u, fma(bj, vj, mul(bk, vk)));
+  float2 F[8], U[8];
+  U[L_RHO] = d;
+  U[L_BI] = bi;
+  U[L_BJ] = bj;
+  U[L_BK] = bk;
+  U[L_VI] = mi;
+  U[L_VJ] = mj;
+  U[L_VK] = mk;
+  U[L_E] = E;
+  F[L_RHO] = mi;
+  F[L_BI] = s2(0.0f);
+  F[L_BJ] = sub(mul(bj, u), mul(bi, vj));
+  F[L_BK] = sub(mul(bk, u), mul(bi, vk));
+  F[L_VI] = fma(mi, u, sub(pt, mul(bi, bi)));
+  F[L_VJ] = sub(mul(mi, vj), mul(bj, bi));
+  F[L_VK] = sub(mul(mi, vk), mul(bk, bi));
+  F[L_E] = sub(mul(add(E, pt), u), mul(vb, bi));
+  // Einfeldt speeds: fast speeds, Roe averages, Roe fast speed
+  const float2 c2 = mul(mul(s2(g), p), inv_d);
+  const float2 va2 = mul(b2, inv_d);
+  const float2 vac2 = mul(mul(bi, bi), inv_d);
+  const float2 sfs = add(c2, va2);
+  const float2 disc = fma(sfs, sfs, mul(mul(s2(-4.0f), c2), vac2));
+  const float2 cfh = mul(HALF, add(sfs, f2(sqrtf(disc.x), sqrtf(disc.y))));
+  const float left_speed = u.x - sqrtf(cfh.x), right_speed = u.y + sqrtf(cfh.y);
+  const float2 sq = f2(sqrtf(d.x), sqrtf(d.y));
+  const float inv_tot = 1.0f / (sq.x + sq.y);
+  const float2 su = mul(sq, u), sv = mul(sq, vj), sw = mul(sq, vk);
+  const float vi_roe = (su.x + su.y) * inv_tot;
+  const float vj_roe = (sv.x + sv.y) * inv_tot;
+  const float vk_roe = (sw.x + sw.y) * inv_tot;
+  const float v_roe2 = vi_roe * vi_roe + vj_roe * vj_roe + vk_roe * vk_roe;
+  const float2 sh = mul(sq, mul(add(E, pt), inv_d));
+  const float h_roe = (sh.x + sh.y) * inv_tot;
+  const float rho_roe = sq.x * sq.y;
+  const float inv_rho_roe = 1.0f / rho_roe;
+  const float bi_roe = bi.x;
+  const float bj_roe = (sq.x * bj.y + sq.y * bj.x) * inv_tot;
+  const float bk_roe = (sq.x * bk.y + sq.y * bk.x) * inv_tot;
+  const float bt_roe2 = bj_roe * bj_roe + bk_roe * bk_roe;
+  const float b_roe2 = bi_roe * bi_roe + bt_roe2;
+  const float dbj = bj.x - bj.y, dbk = bk.x - bk.y;
+  const float x_prime = (dbj * dbj + dbk * dbk) * 0.5f * (gm1 - 1.0f) * inv_tot;
+  const float y_prime = (gm1 - 1.0f) * (d.x + d.y) * 0.5f * inv_rho_roe;
+  const float tilde_a2 = gm1 * (h_roe - 0.5f * v_roe2 - b_roe2 * inv_rho_roe) - x_prime;
+  const float tilde_vai2 = bi_roe * bi_roe * inv_rho_roe;
+  const float tilde_va2 = tilde_vai2 + (gm1 - y_prime) * bt_roe2 * inv_rho_roe;
+  const float sr = tilde_a2 + tilde_va2;
+  const float c_roe =
+      sqrtf(0.5f * (tilde_a2 + tilde_va2 + sqrtf(sr * sr - 4.0f * tilde_a2 * tilde_vai2)));
+  const float bp = fmaxf(fmaxf(vi_roe + c_roe, right_speed), 0.0f);
+  const float bm = fminf(fminf(vi_roe - c_roe, left_speed), 0.0f);
+  const float inv_speed_diff = 1.0f / (bp - bm);
+  const float bpbm = bp * bm;
+  const float2 BPM = f2(bp, -bm);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float2 t = mul(BPM, F[k]);
+    out.f[k] = ((t.x + t.y) + (U[k].y - U[k].x) * bpbm) * inv_speed_diff;
+  }
+  out.eflux = eint_flux(g, d.x, p.x, d.y, p.y, out.f[L_RHO]);
+  out.vbar = (bp * u.x - bm * u.y) * inv_speed_diff;
+}
+
 // HLLC in FP32 (EnzoRiemannHLLC.hpp:34-172 with the Einfeldt speeds of
 // EnzoRiemannHLL.hpp:44-172): the same states, speeds and flux as the FP64
 // form, the left and right states in the two lanes of packed FP32
