@@ -2,6 +2,7 @@
 // kernel templates for one precision R.  Included once per precision TU.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 
 #include "vlct_aux.cuh"
 #include "vlct_launch.h"
@@ -11,6 +12,47 @@
 namespace vlct {
 
 namespace {
+typedef void (*StageKernelFn)(const StageBlock<VLCT_REAL>*, const StageTile*, int, StageInfo,
+                              PhysParams);
+
+// Stage kernels compiled for one tile layout (stage_kernel's LX, LY): the
+// FP32 tiles of the production workloads, where the constant shared-memory
+// layout saves about 4% of a stage.
+//   - 32^3 blocks with 3 ghost zones, MHD (HLLD): the half-dt stage's
+//     region of 36 x 36 columns in tiles of 18 x 9, the full-dt stage's
+//     34 x 34 in tiles of at most 17 x 12 (both the default tiles and the
+//     autotuner's choice for this block);
+//   - 32^3 blocks with 4 ghost zones, hydro (HLLC), the default tiles:
+//     38 x 38 columns in tiles of at most 19 x 10, and 36 x 36 in tiles of
+//     18 x 12, with and without flux storing.
+// Returns null when no such kernel matches the launch's largest tile.
+template <int SOLVER, int RECON, bool DE, int EXTRA>
+StageKernelFn fixed_layout(int tx, int ty) {
+  if constexpr (std::is_same<VLCT_REAL, float>::value && !DE) {
+    if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_NN && EXTRA == EXTRA_NONE) {
+      if (tx == 18 && ty == 9) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 18, 9>;
+    }
+    if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_PLM && EXTRA == EXTRA_NONE) {
+      if (tx == 17 && ty == 12) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 17, 12>;
+    }
+    if constexpr (SOLVER == SOLVER_HLLC && RECON == RECON_NN && EXTRA == EXTRA_NONE) {
+      if (tx == 19 && ty == 10) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 19, 10>;
+    }
+    if constexpr (SOLVER == SOLVER_HLLC && RECON == RECON_PLM && EXTRA != EXTRA_ALL) {
+      if (tx == 18 && ty == 12) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 18, 12>;
+    }
+  }
+  (void)tx;
+  (void)ty;
+  return nullptr;
+}
+
+template <int SOLVER, int RECON, bool DE, int EXTRA>
+StageKernelFn stage_fn(int tx, int ty) {
+  const StageKernelFn f = fixed_layout<SOLVER, RECON, DE, EXTRA>(tx, ty);
+  return f ? f : stage_kernel<VLCT_REAL, SOLVER, RECON, DE, EXTRA>;
+}
+
 template <class R, int SOLVER, int RECON, bool DE>
 cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
                       const StageInfo& info, const PhysParams& phys, int grid,
@@ -20,13 +62,13 @@ cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
   const size_t smem = stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty);
   // the flux-storing-only variant exists for the hydro solver (flux
   // correction is hydro only); the others take the full variant
-  auto k = all ? stage_kernel<R, SOLVER, RECON, DE, EXTRA_ALL>
-               : stage_kernel<R, SOLVER, RECON, DE, EXTRA_NONE>;
+  StageKernelFn k = all ? stage_fn<SOLVER, RECON, DE, EXTRA_ALL>(info.tx, info.ty)
+                        : stage_fn<SOLVER, RECON, DE, EXTRA_NONE>(info.tx, info.ty);
   if (fc && !all) {
     if constexpr (SOLVER == SOLVER_HLLC)
-      k = stage_kernel<R, SOLVER, RECON, DE, EXTRA_FC>;
+      k = stage_fn<SOLVER, RECON, DE, EXTRA_FC>(info.tx, info.ty);
     else
-      k = stage_kernel<R, SOLVER, RECON, DE, EXTRA_ALL>;
+      k = stage_fn<SOLVER, RECON, DE, EXTRA_ALL>(info.tx, info.ty);
   }
   cudaError_t e = cudaFuncSetAttribute(
       k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

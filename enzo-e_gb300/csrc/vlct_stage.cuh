@@ -167,7 +167,12 @@ enum { EXTRA_NONE = 0, EXTRA_FC = 1, EXTRA_ALL = 2 };
 // cost ~4% of a stage); EXTRA_FC can store the boundary fluxes; EXTRA_ALL
 // can also add the gravity source and write the density fluxes that
 // passive_kernel advects the passive scalars with.
-template <class R, int SOLVER, int RECON, bool DE, int EXTRA>
+// LX, LY: when nonzero, the launch's largest tile (info.tx x info.ty) known
+// at compile time and equal to LX x LY.  The shared-memory pitches and
+// region offsets are then constants, so most shared-memory addresses need
+// no run-time arithmetic; tiles smaller than LX x LY (at a block's edge)
+// are handled as in the run-time layout.
+template <class R, int SOLVER, int RECON, bool DE, int EXTRA, int LX = 0, int LY = 0>
 __global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
                                   StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
@@ -179,7 +184,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
   SmemLayout Ls;
-  Ls.init(info.tx, info.ty, RP, NRING, NF);
+  Ls.init(LX > 0 ? LX : info.tx, LY > 0 ? LY : info.ty, RP, NRING, NF);
   // passive scalars (EXTRA_ALL only) are advected by passive_kernel after
   // this kernel, with the density flux of every face written here
   const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;

@@ -16,7 +16,11 @@ refresh, two stages), against the oracle's cycle
     cycle (cycle 1 from the initial state; cycle 2 from the oracle's own
     cycle-1 state rounded to float), and normalised div B (|div B| dx /
     max |B|) <= 1e-6, at the autotuned tiles and at the bench's forced
-    tiles.
+    tiles;
+  - the stage kernels compiled for the bench's tiles (a constant shared-
+    memory layout) give the FP32 state of the run-time layout bit for bit:
+    the MHD box here, and hydro (HLLC) leaves of 32^3 with 4 ghost layers on
+    a two-level mesh, with and without flux storing and correction.
 """
 import ctypes
 
@@ -150,3 +154,58 @@ def test_fp32_error_per_cycle_at_bench_shape(box, oracle_run, tiles):
     err = _field_errors(bt, states[1])
     assert max(err.values()) <= FP32_TOL, err
     assert _divb(bt, w) <= DIVB_TOL
+
+
+def _state(bt):
+    return [bt.download(i) for i in range(bt.n)]
+
+
+def test_fp32_fixed_layout_tiles_equal_runtime_layout(box):
+    # (30, 10) / (28, 14) split the 36- and 34-wide column regions of a 32^3
+    # block into tiles of 18 x 9 and at most 17 x 12, the layouts compiled
+    # as constants; (16, 8) / (12, 12) give 12 x 8 and 12 x 12 (run-time)
+    a, _ = _batch(box, capi.MHD_DTYPE_F32, ((30, 10, 0), (28, 14, 0)))
+    b, _ = _batch(box, capi.MHD_DTYPE_F32, ((16, 8, 0), (12, 12, 0)))
+    assert _run(a, 2) == _run(b, 2)
+    for i, (ga, gb) in enumerate(zip(_state(a), _state(b))):
+        for k in KEYS:
+            assert np.array_equal(ga[k], gb[k]), (i, k)
+
+
+@pytest.mark.parametrize("fc", [False, True])
+def test_fp32_fixed_layout_hydro_leaves_equal_runtime_layout(fc):
+    # the static-mesh-refinement workload's leaves: 32^3 with 4 ghost layers;
+    # the default FP32 tiles (34 x 10 / 24 x 16) split the 38- and 36-wide
+    # regions into tiles of at most 19 x 10 and 18 x 12 (compiled layouts)
+    from test_flux_correct_oracle import smr_blocks
+    nn, g = 32, 4
+    mesh, oblocks, _ = smr_blocks(nn, g)
+    meth = B.EnzoMethodMHDVlct(mhd_choice="no_bfield", riemann_solver="hllc",
+                               reconstruct_method="plm", courant=0.4)
+    L = capi.lib()
+    farr, nf = mesh.face_array()
+    cons = capi.MHD_CONSERVATIVE_DEFAULT
+    names = ("density", "velocity_x", "velocity_y", "velocity_z", "total_energy")
+    onames = ("rho", "vx", "vy", "vz", "etot")
+    out = []
+    for tiles in (((34, 10, 0), (24, 16, 0)), ((16, 8, 0), (12, 12, 0))):
+        bt = Batch(meth, [(nn,) * 3] * len(oblocks), [ob.widths for ob in oblocks],
+                   dtype=capi.MHD_DTYPE_F32, ghost=g)
+        for i, ob in enumerate(oblocks):
+            bt.upload(i, {k: ob.f[o] for k, o in zip(names, onames)})
+        capi.check(L.mhdvlct_batch_set_refresh_faces(bt.h, farr, nf, cons), meth.handle,
+                   "faces")
+        if fc:
+            capi.check(L.mhdvlct_batch_set_flux_correction(bt.h, 0b11111, farr, nf, cons),
+                       meth.handle, "flux correction")
+        for s_, (tx, ty, zc) in enumerate(tiles):
+            capi.check(L.mhdvlct_batch_set_stage_tile(bt.h, s_, tx, ty, zc, 256),
+                       meth.handle, "tile")
+        capi.check(L.mhdvlct_batch_refresh(bt.h, None), meth.handle, "refresh")
+        t = ctypes.c_double()
+        capi.check(L.mhdvlct_batch_run(bt.h, 2, 0, ctypes.byref(t), None), meth.handle, "run")
+        out.append((t.value, _state(bt)))
+    assert out[0][0] == out[1][0]
+    for i, (ga, gb) in enumerate(zip(out[0][1], out[1][1])):
+        for k in names:
+            assert np.array_equal(ga[k], gb[k]), (i, k)
