@@ -75,6 +75,8 @@ struct mhdvlct_batch {
   StageTile* d_tiles[2] = {nullptr, nullptr};
   int ntiles[2] = {0, 0};
   int tile_tx[2] = {0, 0}, tile_ty[2] = {0, 0};
+  int tile_full[2] = {0, 0};  // 1: every tile of the stage is tile_tx x tile_ty
+  int block_m = 0;            // every block's extent along all axes, if equal; else 0
   int* d_queue = nullptr;     // 2 counters
   int* d_nbr = nullptr;
   // mesh refresh from a face list (replaces the 27-neighbour same-level
@@ -290,6 +292,19 @@ int build_descriptors(mhdvlct_batch* b, cudaStream_t st) {
       }
     }
   }
+  // the launch shape: every tile at the largest extent; one cubic extent
+  // shared by every block
+  int block_m = b->off[0].m[0];
+  for (int i = 0; i < b->nblocks; i++)
+    for (int a = 0; a < 3; a++)
+      if (b->off[i].m[a] != block_m) block_m = 0;
+  b->block_m = block_m;
+  for (int s = 0; s < 2; s++) {
+    b->tile_full[s] = 1;
+    for (auto& o : order[s])
+      if (o.second.xb - o.second.xa != tx[s] || o.second.yb - o.second.ya != ty[s])
+        b->tile_full[s] = 0;
+  }
   for (int s = 0; s < 2; s++) {
     std::stable_sort(order[s].begin(), order[s].end(),
                      [](const std::pair<double, StageTile>& a,
@@ -355,6 +370,8 @@ StageInfo batch_stage_info(const mhdvlct_batch* b, int s, int* queue) {
   // (EnzoMHDIntegratorStageCommands.cpp:279)
   info.gravity = s == 1 ? b->gravity : 0;
   info.npass = b->npass;
+  info.full_tiles = b->tile_full[s];
+  info.block_m = b->block_m;
   return info;
 }
 

@@ -15,41 +15,54 @@ namespace {
 typedef void (*StageKernelFn)(const StageBlock<VLCT_REAL>*, const StageTile*, int, StageInfo,
                               PhysParams);
 
-// Stage kernels compiled for one tile layout (stage_kernel's LX, LY): the
-// FP32 tiles of the production workloads, where the constant shared-memory
-// layout saves about 4% of a stage.
-//   - 32^3 blocks with 3 ghost zones, MHD (HLLD): the half-dt stage's
-//     region of 36 x 36 columns in tiles of 18 x 9, the full-dt stage's
-//     34 x 34 in tiles of at most 17 x 12 (both the default tiles and the
-//     autotuner's choice for this block);
-//   - 32^3 blocks with 4 ghost zones, hydro (HLLC), the default tiles:
-//     38 x 38 columns in tiles of at most 19 x 10, and 36 x 36 in tiles of
-//     18 x 12, with and without flux storing.
-// Returns null when no such kernel matches the launch's largest tile.
+// Stage kernels compiled for one launch shape (FixedShape: tile, block
+// extent, stale depths as constants), for the FP32 launches of the
+// production workloads, where the constants save about 12% of a stage:
+//   - 32^3 blocks with 3 ghost zones (extent 38), MHD (HLLD), the two-stage
+//     scheme with NN then PLM: the half-dt stage's 36 x 36 columns in tiles
+//     of 18 x 9, the full-dt stage's 34 x 34 in tiles of at most 17 x 12
+//     (both the default tiles and the autotuner's choice for this block);
+//   - 32^3 blocks with 4 ghost zones (extent 40), hydro (HLLC), the default
+//     tiles: 38 x 38 columns in tiles of at most 19 x 10, and 36 x 36 in
+//     tiles of 18 x 12, with and without flux storing.
+// Returns null unless the launch has exactly one of these shapes.
 template <int SOLVER, int RECON, bool DE, int EXTRA>
-StageKernelFn fixed_layout(int tx, int ty) {
+StageKernelFn fixed_shape(const StageInfo& in) {
   if constexpr (std::is_same<VLCT_REAL, float>::value && !DE) {
+    // the launch's (tile, every-tile-full, block extent, s, S, final) against
+    // one compiled shape
+    auto is = [&](int lx, int ly, bool full, int bm, int s, int S, bool fin) {
+      return in.tx == lx && in.ty == ly && (!full || in.full_tiles) && in.block_m == bm &&
+             in.s == s && in.S == S && (in.final_stage != 0) == fin;
+    };
     if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_NN && EXTRA == EXTRA_NONE) {
-      if (tx == 18 && ty == 9) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 18, 9>;
+      if (is(18, 9, true, 38, 0, 0, false))
+        return stage_kernel<float, SOLVER, RECON, DE, EXTRA,
+                            FixedShape<18, 9, true, 38, 0, 0, false>>;
     }
     if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_PLM && EXTRA == EXTRA_NONE) {
-      if (tx == 17 && ty == 12) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 17, 12>;
+      if (is(17, 12, false, 38, 1, 2, true))
+        return stage_kernel<float, SOLVER, RECON, DE, EXTRA,
+                            FixedShape<17, 12, false, 38, 1, 2, true>>;
     }
     if constexpr (SOLVER == SOLVER_HLLC && RECON == RECON_NN && EXTRA == EXTRA_NONE) {
-      if (tx == 19 && ty == 10) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 19, 10>;
+      if (is(19, 10, false, 40, 0, 0, false))
+        return stage_kernel<float, SOLVER, RECON, DE, EXTRA,
+                            FixedShape<19, 10, false, 40, 0, 0, false>>;
     }
     if constexpr (SOLVER == SOLVER_HLLC && RECON == RECON_PLM && EXTRA != EXTRA_ALL) {
-      if (tx == 18 && ty == 12) return stage_kernel<float, SOLVER, RECON, DE, EXTRA, 18, 12>;
+      if (is(18, 12, true, 40, 1, 2, true))
+        return stage_kernel<float, SOLVER, RECON, DE, EXTRA,
+                            FixedShape<18, 12, true, 40, 1, 2, true>>;
     }
   }
-  (void)tx;
-  (void)ty;
+  (void)in;
   return nullptr;
 }
 
 template <int SOLVER, int RECON, bool DE, int EXTRA>
-StageKernelFn stage_fn(int tx, int ty) {
-  const StageKernelFn f = fixed_layout<SOLVER, RECON, DE, EXTRA>(tx, ty);
+StageKernelFn stage_fn(const StageInfo& info) {
+  const StageKernelFn f = fixed_shape<SOLVER, RECON, DE, EXTRA>(info);
   return f ? f : stage_kernel<VLCT_REAL, SOLVER, RECON, DE, EXTRA>;
 }
 
@@ -62,13 +75,13 @@ cudaError_t stage_one(const StageBlock<R>* b, const StageTile* t, int nt,
   const size_t smem = stage_smem_bytes<R, SOLVER, RECON, DE>(info.tx, info.ty);
   // the flux-storing-only variant exists for the hydro solver (flux
   // correction is hydro only); the others take the full variant
-  StageKernelFn k = all ? stage_fn<SOLVER, RECON, DE, EXTRA_ALL>(info.tx, info.ty)
-                        : stage_fn<SOLVER, RECON, DE, EXTRA_NONE>(info.tx, info.ty);
+  StageKernelFn k = all ? stage_fn<SOLVER, RECON, DE, EXTRA_ALL>(info)
+                        : stage_fn<SOLVER, RECON, DE, EXTRA_NONE>(info);
   if (fc && !all) {
     if constexpr (SOLVER == SOLVER_HLLC)
-      k = stage_fn<SOLVER, RECON, DE, EXTRA_FC>(info.tx, info.ty);
+      k = stage_fn<SOLVER, RECON, DE, EXTRA_FC>(info);
     else
-      k = stage_fn<SOLVER, RECON, DE, EXTRA_ALL>(info.tx, info.ty);
+      k = stage_fn<SOLVER, RECON, DE, EXTRA_ALL>(info);
   }
   cudaError_t e = cudaFuncSetAttribute(
       k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

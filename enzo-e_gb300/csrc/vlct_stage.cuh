@@ -163,16 +163,33 @@ inline int stage_max_threads(int recon) {
 
 enum { EXTRA_NONE = 0, EXTRA_FC = 1, EXTRA_ALL = 2 };
 
+// Launch shapes of the stage kernel.  RuntimeShape takes every value from
+// the launch.  FixedShape<LX, LY, FULL, BM, s, S, FINAL> is a launch whose
+// largest tile is LX x LY (every tile exactly that when FULL), whose blocks
+// all have extent BM (ghosts included) along each axis, and whose stage has
+// stale depths s (start) and S (after reconstruction) and is the final
+// stage when FINAL.  A fixed-shape kernel runs only launches of exactly
+// that shape; its arithmetic is the run-time kernel's.
+struct RuntimeShape {
+  static constexpr int LX = 0, LY = 0, BM = 0, s = -1, S = -1;
+  static constexpr bool FULL = false, FINAL = false;
+};
+template <int LX_, int LY_, bool FULL_, int BM_, int s_, int S_, bool FINAL_>
+struct FixedShape {
+  static_assert(LX_ > 0 && LY_ > 0 && BM_ > 0 && s_ >= 0 && S_ >= s_, "fixed shape");
+  static constexpr int LX = LX_, LY = LY_, BM = BM_, s = s_, S = S_;
+  static constexpr bool FULL = FULL_, FINAL = FINAL_;
+};
+
 // EXTRA: EXTRA_NONE compiles the optional work out (its run-time checks alone
 // cost ~4% of a stage); EXTRA_FC can store the boundary fluxes; EXTRA_ALL
 // can also add the gravity source and write the density fluxes that
 // passive_kernel advects the passive scalars with.
-// LX, LY: when nonzero, the launch's largest tile (info.tx x info.ty) known
-// at compile time and equal to LX x LY.  The shared-memory pitches and
-// region offsets are then constants, so most shared-memory addresses need
-// no run-time arithmetic; tiles smaller than LX x LY (at a block's edge)
-// are handled as in the run-time layout.
-template <class R, int SOLVER, int RECON, bool DE, int EXTRA, int LX = 0, int LY = 0>
+// SH: the launch's shape -- RuntimeShape (everything read from the launch's
+// StageInfo and the block descriptors) or a FixedShape, whose values are
+// compile-time constants so that the index arithmetic of shared- and
+// global-memory accesses folds.
+template <class R, int SOLVER, int RECON, bool DE, int EXTRA, class SH = RuntimeShape>
 __global__ void __launch_bounds__(StageBounds<R, RECON>::threads,
                                   StageBounds<R, RECON>::min_blocks)
 stage_kernel(const StageBlock<R>* __restrict__ blocks,
@@ -184,7 +201,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
   SmemLayout Ls;
-  Ls.init(LX > 0 ? LX : info.tx, LY > 0 ? LY : info.ty, RP, NRING, NF);
+  Ls.init(SH::LX > 0 ? SH::LX : info.tx, SH::LY > 0 ? SH::LY : info.ty, RP, NRING, NF);
   // passive scalars (EXTRA_ALL only) are advected by passive_kernel after
   // this kernel, with the density flux of every face written here
   const int PP = Ls.PP, QP = Ls.QP, HP = Ls.HP, G = Ls.G;
@@ -199,7 +216,8 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   R* s_ez = sm + Ls.o_ez;
   R* s_bz = sm + Ls.o_bz;
   const int tid = threadIdx.x, nthr = blockDim.x;
-  const int s = info.s, S = info.S;
+  const int s = SH::S >= 0 ? SH::s : info.s, S = SH::S >= 0 ? SH::S : info.S;
+  const bool final_stage = SH::S >= 0 ? SH::FINAL : info.final_stage != 0;
   const R g = R(phys.gamma);
   const R theta = R(phys.theta_limiter);
   const R dfloor = R(phys.density_floor), pfloor = R(phys.pressure_floor);
@@ -232,7 +250,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
           reinterpret_cast<const unsigned long long*>(blocks + tl.block);
       for (int w = tid; w < (int)((sizeof(StageBlock<R>) + 7) / 8); w += nthr)
         s_blk_raw[w] = src[w];
-      if (EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc)) {
+      if (EXTRA != EXTRA_NONE && final_stage && (info.fc != nullptr || info.block_fc)) {
         const void* fsrc = blocks[tl.block].fc != nullptr ? blocks[tl.block].fc : info.fc;
         const unsigned long long* fw = reinterpret_cast<const unsigned long long*>(fsrc);
         for (int w = tid; w < kFoWords; w += nthr) s_fo_raw[w] = fw[w];
@@ -240,9 +258,11 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     }
     const StageBlock<R>& B = *reinterpret_cast<const StageBlock<R>*>(s_blk_raw);
     const StageBlock<R>& Bg = blocks[tl.block];
-    const int m0 = Bg.m[0], m1 = Bg.m[1], m2 = Bg.m[2];
+    const int m0 = SH::BM > 0 ? SH::BM : Bg.m[0];
+    const int m1 = SH::BM > 0 ? SH::BM : Bg.m[1];
+    const int m2 = SH::BM > 0 ? SH::BM : Bg.m[2];
     const int xa = tl.xa, xb = tl.xb, ya = tl.ya, yb = tl.yb;
-    const int tx = xb - xa, ty = yb - ya;
+    const int tx = SH::FULL ? SH::LX : xb - xa, ty = SH::FULL ? SH::LY : yb - ya;
     // dt / dx per axis, once per tile (FP64 divisions: one thread)
     if (tid == 0) {
       const double dt = *Bg.dt * info.dt_factor;
@@ -254,9 +274,9 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     __syncthreads();  // also publishes the descriptor copy
     const R dtdx[3] = {s_dtdx[0], s_dtdx[1], s_dtdx[2]};
     // output window of centred B (and the z-march range)
-    const int olo = info.final_stage ? S : S + 1;
-    const int ohi_x = info.final_stage ? m0 - S : m0 - S - 1;
-    const int ohi_y = info.final_stage ? m1 - S : m1 - S - 1;
+    const int olo = final_stage ? S : S + 1;
+    const int ohi_x = final_stage ? m0 - S : m0 - S - 1;
+    const int ohi_y = final_stage ? m1 - S : m1 - S - 1;
     const int za = tl.za, zb = tl.zb;  // output planes of this chunk
     const int t0 = za - 1;
     // prim-tile origin and halo-grid origin
@@ -483,7 +503,7 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     // (the outputs are looked up inside the pass: nothing extra stays live
     // across the z-march)
     const bool store_fc =
-        EXTRA != EXTRA_NONE && info.final_stage && (info.fc != nullptr || info.block_fc);
+        EXTRA != EXTRA_NONE && final_stage && (info.fc != nullptr || info.block_fc);
     auto store_fluxes = [&](int t, bool zfaces, int pl) {
       const FluxOut<R>* fo = reinterpret_cast<const FluxOut<R>*>(s_fo_raw);
       const int gg = info.fc_g;

@@ -80,6 +80,11 @@ struct StageInfo {
                              // boundary fluxes are stored; null otherwise
   int block_fc = 0;          // 1: the blocks carry their own FluxOut (StageBlock::fc)
   int fc_g = 0;              // ghost depth of the blocks whose fluxes are stored
+  // shape of the launch, for the stage kernels compiled with it as constants
+  // (zero: not known, the run-time shape is used)
+  int full_tiles = 0;        // 1: every tile of the launch is tx x ty
+  int block_m = 0;           // every block's extent (ghosts included) along all
+                             // three axes, when they are all equal
 };
 
 // Boundary fluxes for flux correction (EnzoMethodMHDVlct.cpp:250-330):
