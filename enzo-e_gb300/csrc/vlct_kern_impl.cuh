@@ -21,7 +21,8 @@ typedef void (*StageKernelFn)(const StageBlock<VLCT_REAL>*, const StageTile*, in
 //   - 32^3 blocks with 3 ghost zones (extent 38), MHD (HLLD), the two-stage
 //     scheme with NN then PLM: the half-dt stage's 36 x 36 columns in tiles
 //     of 18 x 9, the full-dt stage's 34 x 34 in tiles of at most 17 x 12
-//     (both the default tiles and the autotuner's choice for this block);
+//     (both the default tiles and the autotuner's choice for this block),
+//     plain and with the gravity source / passive scalars;
 //   - 32^3 blocks with 4 ghost zones (extent 40), hydro (HLLC), the default
 //     tiles: 38 x 38 columns in tiles of at most 19 x 10, and 36 x 36 in
 //     tiles of 18 x 12, with and without flux storing.
@@ -35,12 +36,12 @@ StageKernelFn fixed_shape(const StageInfo& in) {
       return in.tx == lx && in.ty == ly && (!full || in.full_tiles) && in.block_m == bm &&
              in.s == s && in.S == S && (in.final_stage != 0) == fin;
     };
-    if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_NN && EXTRA == EXTRA_NONE) {
+    if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_NN && EXTRA != EXTRA_FC) {
       if (is(18, 9, true, 38, 0, 0, false))
         return stage_kernel<float, SOLVER, RECON, DE, EXTRA,
                             FixedShape<18, 9, true, 38, 0, 0, false>>;
     }
-    if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_PLM && EXTRA == EXTRA_NONE) {
+    if constexpr (SOLVER == SOLVER_HLLD && RECON == RECON_PLM && EXTRA != EXTRA_FC) {
       if (is(17, 12, false, 38, 1, 2, true))
         return stage_kernel<float, SOLVER, RECON, DE, EXTRA,
                             FixedShape<17, 12, false, 38, 1, 2, true>>;

@@ -17,8 +17,9 @@
 //      plane t -- centred B, flux divergence + dual-energy source, density
 //      floor, energy floor / dual-energy sync, store -- and the primitives
 //      + cell-centred E of plane t+1+L (L = 1 for NN, 2 for PLM) loaded into
-//      the ring for the next plane (in the PLM stages the raw fields are
-//      copied asynchronously right after B and converted here).
+//      the ring for the next plane (in the PLM stages, and in NN stages
+//      compiled for a fixed launch shape, the raw fields are copied
+//      asynchronously right after B and converted here).
 //
 // The index windows of every quantity are those of the reference's array
 // passes (EnzoMHDIntegratorStageCommands::compute_update_stage,
@@ -297,10 +298,12 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
     // exactly the cells it issued, so the two need no barrier between them;
     // in the z-march the copies of plane t+1+L go out right after phase B of
     // plane t (the slot they overwrite, plane t-1's, is no longer read) and
-    // land while phases C and D run.  The NN stage, already close to its
-    // issue limit, loads in finish_plane directly: the extra shared-memory
-    // pass costs it more than the latency it would hide.
-    constexpr bool ASYNC_LOADS = RECON != RECON_NN;
+    // land while phases C and D run.  The NN stage with the run-time shape,
+    // already close to its issue limit, loads in finish_plane directly: the
+    // extra shared-memory pass costs it more than the latency it would hide.
+    // With a fixed shape it issues fewer instructions, and the asynchronous
+    // copies pay there too.
+    constexpr bool ASYNC_LOADS = RECON != RECON_NN || SH::BM > 0;
     auto issue_plane = [&](int p) {
       if (!ASYNC_LOADS || !inr(p, s, m2 - s)) return;
       const int slot = p % NRING;

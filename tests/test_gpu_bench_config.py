@@ -17,10 +17,12 @@ refresh, two stages), against the oracle's cycle
     cycle-1 state rounded to float), and normalised div B (|div B| dx /
     max |B|) <= 1e-6, at the autotuned tiles and at the bench's forced
     tiles;
-  - the stage kernels compiled for the bench's tiles (a constant shared-
-    memory layout) give the FP32 state of the run-time layout bit for bit:
-    the MHD box here, and hydro (HLLC) leaves of 32^3 with 4 ghost layers on
-    a two-level mesh, with and without flux storing and correction.
+  - the stage kernels compiled for the bench's launch shape (tiles, block
+    extent and stale depths as constants) give the FP32 state of the
+    run-time kernels bit for bit: the MHD box here, plain and with the
+    gravity source and two passive scalars, and hydro (HLLC) leaves of 32^3
+    with 4 ghost layers on a two-level mesh, with and without flux storing
+    and correction.
 """
 import ctypes
 
@@ -169,6 +171,43 @@ def test_fp32_fixed_layout_tiles_equal_runtime_layout(box):
     assert _run(a, 2) == _run(b, 2)
     for i, (ga, gb) in enumerate(zip(_state(a), _state(b))):
         for k in KEYS:
+            assert np.array_equal(ga[k], gb[k]), (i, k)
+
+
+def test_fp32_fixed_layout_extras_equal_runtime_layout(box):
+    # the same tiles with the gravity source and two passive scalars (the
+    # instantiation that writes the density fluxes for passive_kernel)
+    blocks, w = box
+    rng = np.random.default_rng(23)
+    m = n + 2 * G
+    states = []
+    for st in blocks:
+        st = dict(st)
+        for k in ("acceleration_x", "acceleration_y", "acceleration_z"):
+            st[k] = np.zeros((m, m, m))
+            st[k][ACT] = 0.3 * (rng.random((n, n, n)) - 0.5)
+        for k in range(2):
+            st[f"passive_{k}"] = st["density"] * (0.2 + 0.6 * rng.random((m, m, m)))
+        states.append(st)
+    meth = B.EnzoMethodMHDVlct(riemann_solver="hlld", reconstruct_method="plm",
+                               courant=COURANT)
+    L = capi.lib()
+    nbr = ic.brick_neighbors(NB)
+    out = []
+    for tiles in (((30, 10, 0), (28, 14, 0)), ((16, 8, 0), (12, 12, 0))):
+        bt = Batch(meth, [(n, n, n)] * NBLK, [w] * NBLK, dtype=capi.MHD_DTYPE_F32,
+                   npassive=2, gravity=True)
+        capi.check(L.mhdvlct_batch_set_neighbors(
+            bt.h, (ctypes.c_int * nbr.size)(*nbr.ravel().tolist())))
+        for i, st in enumerate(states):
+            bt.upload(i, st)
+        for s_, (tx, ty, zc) in enumerate(tiles):
+            capi.check(L.mhdvlct_batch_set_stage_tile(bt.h, s_, tx, ty, zc, 256),
+                       meth.handle, "tile")
+        out.append((_run(bt, 2), _state(bt)))
+    assert out[0][0] == out[1][0]
+    for i, (ga, gb) in enumerate(zip(out[0][1], out[1][1])):
+        for k in KEYS + ("passive_0", "passive_1"):
             assert np.array_equal(ga[k], gb[k]), (i, k)
 
 
