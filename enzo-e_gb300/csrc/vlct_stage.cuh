@@ -36,6 +36,8 @@
 // advected by passive_kernel, vlct_passive.cuh); the default one compiles
 // all of these out.
 #pragma once
+#include <type_traits>
+
 #include "vlct_energy.cuh"
 #include "vlct_physics.cuh"
 #include "vlct_types.h"
@@ -219,11 +221,20 @@ stage_kernel(const StageBlock<R>* __restrict__ blocks,
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int s = SH::S >= 0 ? SH::s : info.s, S = SH::S >= 0 ? SH::S : info.S;
   const bool final_stage = SH::S >= 0 ? SH::FINAL : info.final_stage != 0;
-  const R g = R(phys.gamma);
-  const R theta = R(phys.theta_limiter);
-  const R dfloor = R(phys.density_floor), pfloor = R(phys.pressure_floor);
+  // the physical constants in R.  In the FP32 NN stage (registers capped for
+  // three CTAs per SM, so the compiler reloads constants from the
+  // parameters) they are the values rounded on the host, which need no FP64
+  // conversion on the device; the same values as the conversions here.
+  constexpr bool F32 = std::is_same<R, float>::value && RECON == RECON_NN;
+  const R g = F32 ? R(phys.gamma_f) : R(phys.gamma);
+  const R theta = F32 ? R(phys.theta_limiter_f) : R(phys.theta_limiter);
+  const R dfloor = F32 ? R(phys.density_floor_f) : R(phys.density_floor);
+  const R pfloor = F32 ? R(phys.pressure_floor_f) : R(phys.pressure_floor);
   EnergyConsts<R> econ;
-  econ.init(phys.gamma, phys.pressure_floor, DE ? phys.eta : 0.0);
+  if constexpr (F32)
+    econ.init_rounded(phys, DE);
+  else
+    econ.init(phys.gamma, phys.pressure_floor, DE ? phys.eta : 0.0);
   const FastDiv divPP(Ls.PP), divHP(Ls.HP);
 
   __shared__ int s_next;

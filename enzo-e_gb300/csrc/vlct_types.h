@@ -57,10 +57,24 @@ struct PhysParams {
   // derived on the host (set_derived), so that no kernel thread spends FP64
   // divisions on them: gamma - 1, 1 / (gamma - 1), gamma (gamma - 1)
   double gm1 = 0.0, inv_gm1 = 0.0, ggm1 = 0.0;
+  // the FP32 kernels' constants, each rounded once here from the double
+  // above: read from the kernel parameters, they need no FP64 conversion on
+  // the device (GB300's FP64 pipe is narrow)
+  float gamma_f = 0.f, density_floor_f = 0.f, pressure_floor_f = 0.f;
+  float theta_limiter_f = 0.f, eta_f = 0.f;
+  float gm1_f = 0.f, inv_gm1_f = 0.f, ggm1_f = 0.f;
   void set_derived() {
     gm1 = gamma - 1.0;
     inv_gm1 = 1. / (gamma - 1.);
     ggm1 = gamma * (gamma - 1.);
+    gamma_f = (float)gamma;
+    density_floor_f = (float)density_floor;
+    pressure_floor_f = (float)pressure_floor;
+    theta_limiter_f = (float)theta_limiter;
+    eta_f = (float)eta;
+    gm1_f = (float)gm1;
+    inv_gm1_f = (float)inv_gm1;
+    ggm1_f = (float)ggm1;
   }
 };
 
