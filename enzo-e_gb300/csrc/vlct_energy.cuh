@@ -76,9 +76,6 @@ template <class R> struct EnergyConsts {
     eta = R(eta_);
     half_factor = (eta_ != 0.) ? R(0.5) : R(0.);
   }
-  // the same values from the host-derived constants of the physics
-  // parameters, without the FP64 division: for kernels whose threads are
-  // short-lived (the timestep), where it would be a noticeable share
   // FP32 only: the constants rounded on the host (PhysParams::set_derived),
   // the same values as init(gamma, pressure_floor, eta) gives
   __host__ __device__ void init_rounded(const PhysParams& ph, bool de) {
@@ -89,6 +86,9 @@ template <class R> struct EnergyConsts {
     eta = de ? ph.eta_f : 0.f;
     half_factor = (de && ph.eta != 0.) ? 0.5f : 0.f;
   }
+  // the same values from the host-derived constants of the physics
+  // parameters, without the FP64 division: for kernels whose threads are
+  // short-lived (the timestep), where it would be a noticeable share
   __host__ __device__ void init(const PhysParams& ph, bool de) {
     gm1 = R(ph.gm1);
     inv_gm1 = R(ph.inv_gm1);
