@@ -194,7 +194,10 @@ def run_reference(a, rank, world):
     line = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "zone-updates/s", "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+        "warmup": a.warmup,
+        # one cycle of the sampled blocks at the median rate
+        "ms_per_step": sample * n ** 3 / value * 1e3,
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"turbulent box {a.n}^3 in {a.nb ** 3} blocks of {n}^3 "
                                f"(+{GHOST} ghosts), HLLD+PLM, gamma 5/3, CFL {COURANT}, "
